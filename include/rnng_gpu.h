@@ -1,0 +1,160 @@
+/*
+ * rnng_gpu.h - C ABI of the GB300 epsilon-graph / Vietoris-Rips library.
+ *
+ * One shared library (librnng_gpu.so) owns all device work for RNNG's hot path.
+ * The C++ headers next to this file (point.h, search.h, graph.h, simplex.h) keep
+ * RNNG's template API and forward their bulk operations here; Python tests and
+ * the benchmark bind the same entry points through ctypes.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: RNNG_OK (0) or an RNNG_ERR_* code.
+ *     Nothing throws across this boundary.  rnng_last_error() gives the message.
+ *   - Plain pointers and sizes only.  Pointers are host memory unless the call's
+ *     flags say RNNG_INPUT_DEVICE (inputs) / RNNG_OUTPUT_DEVICE (outputs).
+ *   - Results live in library-owned buffers.  With RNNG_OUTPUT_DEVICE they are
+ *     device allocations that stay valid until rnng_edges_free / rnng_simplices_free.
+ *     Otherwise they are host arrays in the context's pinned staging memory, valid
+ *     until the next call on the same context (copy them to keep them); freeing
+ *     them is a no-op.
+ *   - All work of a context is ordered on the context's CUDA stream.  One context
+ *     per host thread; calls on one context must not overlap.
+ *   - Point ids are int64 (RNNG's Index, include/utils.h:24); distances are float
+ *     (RNNG's Real, include/utils.h:25).
+ *
+ * Distances and predicates are those of RNNG's drivers:
+ *   L2   = sqrtf(sum_i (p_i - q_i)^2), float, sequential i = 0..d-1, no FMA
+ *          (drivers/systolic.cpp:253-269); edge iff L2 <= radius.
+ *   edit = Levenshtein distance with unit costs, as a float
+ *          (drivers/systolic.cpp:271-299); edge iff edit <= radius.
+ * Every reported distance is bit-identical to what those functors return.
+ */
+#ifndef RNNG_GPU_H_
+#define RNNG_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define RNNG_OK 0
+#define RNNG_ERR_INVALID 1    /* bad argument (null pointer, negative size, dimension mismatch) */
+#define RNNG_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define RNNG_ERR_NOMEM 3      /* device or host allocation failed */
+#define RNNG_ERR_OVERFLOW 4   /* a result does not fit the representation (e.g. simplex ids) */
+#define RNNG_ERR_DEVICE 5     /* a kernel reported a fault through its error word (e.g. a bounded wait ran out) */
+#define RNNG_ERR_UNSUPPORTED 6
+
+/* flags */
+#define RNNG_INPUT_DEVICE 1u   /* input pointers are device pointers (no host-to-device copy) */
+#define RNNG_OUTPUT_DEVICE 2u  /* leave results on the device (no device-to-host copy) */
+#define RNNG_SORT_OUTPUT 4u    /* sort edges by (u, v) / simplices by (value, id) */
+
+/* L2 tile modes */
+#define RNNG_MODE_FP32_DIRECT 0  /* every candidate pair evaluated with the reference's sequential FP32 L2 */
+#define RNNG_MODE_BF16_RECHECK 1 /* BF16 tensor-core Gram candidates with a rigorous margin, FP32 recheck */
+
+typedef struct rnng_ctx rnng_ctx;
+
+/* Unordered edges u < v with their reference distances, in point-id space. */
+typedef struct rnng_edges {
+    int64_t count;
+    int64_t* u;
+    int64_t* v;
+    float* w;
+    int on_device; /* 1: u, v, w are device pointers owned by the caller */
+    int staged;    /* 1: host arrays in the context's staging memory (not freed by rnng_edges_free) */
+} rnng_edges;
+
+/* A filtration: simplex ids (RNNG's Simplex encoding, include/simplex.hpp:5-19) and values. */
+typedef struct rnng_simplices {
+    int64_t count;
+    int64_t* id;
+    float* value;
+    int on_device;
+    int staged;
+} rnng_simplices;
+
+/* Counters and stage times of the last call on a context (milliseconds). */
+typedef struct rnng_stats {
+    double ms_total, ms_h2d, ms_partition, ms_sort, ms_bounds, ms_prune, ms_tiles, ms_finalize, ms_d2h;
+    int64_t num_cells;      /* landmarks / cells of the partition */
+    int64_t tile_pairs;     /* tile pairs that survived pruning */
+    int64_t tile_pairs_all; /* tile pairs before pruning */
+    int64_t pairs_evaluated;/* point pairs inside surviving tiles */
+    int64_t candidates;     /* BF16 mode: pairs sent to the FP32 recheck */
+    int64_t edges;          /* edges found (u < v) */
+    int64_t retries;        /* edge-buffer regrowths */
+    int64_t simplices;      /* Rips: simplices emitted */
+    int64_t kernel_launches;/* kernels launched by the call */
+} rnng_stats;
+
+/* Context ---------------------------------------------------------------------------------
+ * Replaces nothing in RNNG (which has no device state); it holds the GPU, the stream
+ * and reusable scratch so that steady-state calls do not allocate. */
+int rnng_ctx_create(int device, rnng_ctx** out);
+int rnng_ctx_destroy(rnng_ctx* ctx);
+const char* rnng_last_error(const rnng_ctx* ctx);
+int rnng_get_stats(const rnng_ctx* ctx, rnng_stats* out);
+/* The context's CUDA stream (cudaStream_t), for callers that order their own work with it. */
+int rnng_ctx_stream(rnng_ctx* ctx, void** stream);
+/* Releases all cached scratch memory of the context. */
+int rnng_ctx_trim(rnng_ctx* ctx);
+
+/* Epsilon graph, L2 ------------------------------------------------------------------------
+ * Replaces the neighbour search of the drivers: CoverTree::build + radius_query per point
+ * (drivers/systolic.cpp:96-147, include/search.hpp:6-264) and the landmark pipeline
+ * VoronoiDiagram + add_ghost_points_systolic + per-cell radius_query_batched
+ * (drivers/landmark.cpp:139-210, include/point.hpp:537-929, include/search.hpp:267-340).
+ * X is n x d row-major float32; ids (may be NULL = 0..n-1) are the point ids.
+ * Output: every unordered pair with L2 <= radius, as u < v (ids compared), each once. */
+int rnng_eps_graph_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
+                      int mode, unsigned flags, rnng_edges* out);
+
+/* Radius query of a batch against an indexed set: every (query q, point p) with
+ * L2(p, q) <= radius.  Replaces CoverTree::radius_query_batched
+ * (include/search.hpp:267-340) and BruteForce::radius_query (include/search.hpp:390-407).
+ * out->u holds query ids, out->v point ids (the functor's (q.id(), p.id()) order in
+ * drivers/landmark.cpp:198-201). */
+int rnng_radius_query_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, const float* Q,
+                         const int64_t* qids, int64_t nq, int64_t d, float radius, unsigned flags,
+                         rnng_edges* out);
+
+/* Nearest landmark per point with the reference's tie rule (the last of equal
+ * distances wins): VoronoiDiagram::VoronoiDiagram (include/point.hpp:537-559).
+ * cell[i] in [0, m), dist[i] = L2(center, x_i) bit-identical to the reference. */
+int rnng_voronoi_l2(rnng_ctx* ctx, const float* X, int64_t n, const float* C, int64_t m, int64_t d,
+                    unsigned flags, int64_t* cell, float* dist);
+
+/* Epsilon graph, edit distance -------------------------------------------------------------
+ * Strings in RNNG's CSR layout (include/point.h:77-79): atoms[offsets[i] .. offsets[i+1]).
+ * Replaces the drivers' edit-distance path (drivers/landmark.cpp:61-62 with
+ * EditDistance<char>).  Output as rnng_eps_graph_l2. */
+int rnng_eps_graph_edit(rnng_ctx* ctx, const uint8_t* atoms, const int64_t* offsets, const int64_t* ids,
+                        int64_t n, float radius, unsigned flags, rnng_edges* out);
+
+/* Vietoris-Rips filtration ----------------------------------------------------------------
+ * Replaces VoronoiComplex::build_filtration per cell + merge_and_write_filtration
+ * (include/point.hpp:1136-1267, include/simplex.hpp:130-196, drivers/rips.cpp:174-245):
+ * all vertices (value 0), edges (value = L2) and, for maxdim >= 2, triangles (value =
+ * max edge), ids per include/simplex.hpp:5-19 over the point ids, sorted by (value, id).
+ * maxdim is 0, 1 or 2. */
+int rnng_rips_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
+                 int maxdim, int mode, unsigned flags, rnng_simplices* out);
+
+/* Graph finalisation: Graph(edges) + redistribute_edges at one rank
+ * (include/graph.h:14, include/graph.hpp:59-116): from unordered edges, the list of
+ * both orientations plus the self-loop (i, i, 0) of every vertex 0..num_vertices-1,
+ * sorted by (u, v).  Output count = num_vertices + 2 * edges. */
+int rnng_graph_finalize(rnng_ctx* ctx, const rnng_edges* edges, int64_t num_vertices, unsigned flags,
+                        rnng_edges* out);
+
+int rnng_edges_free(rnng_edges* e);
+int rnng_simplices_free(rnng_simplices* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RNNG_GPU_H_ */

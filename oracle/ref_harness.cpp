@@ -1,0 +1,201 @@
+// Harness that runs RNNG's own CPU path (its headers, compiled from the RNNG source
+// tree with the single-rank MPI shim) and dumps the results in binary, so that edge
+// weights and filtration values can be compared bit for bit.  RNNG's drivers print
+// weights with 6 digits (include/graph.hpp:33, include/simplex.hpp:183), which is
+// not enough to prove bit-exactness; this harness makes the same API calls in the
+// same order as the drivers and writes the functor arguments instead.
+//
+// TEST INFRASTRUCTURE ONLY: built by oracle/Makefile into oracle/_ref/, used to make
+// the golden fixtures under tests/golden/ and to check the C oracle.
+//
+// Modes (all single rank):
+//   systolic <in.fvecs> <radius> <out>          drivers/systolic.cpp:96-147
+//   landmark <l2|edit> <in> <radius> <m> <seed> <out>
+//                                                drivers/landmark.cpp:111-210
+//   rips <in.fvecs> <radius> <maxdim> <m> <seed> <out>
+//                                                drivers/rips.cpp:106-180
+// Edge output: int64 count, then count int64 u, count int64 v, count float32 w
+// (u = query id, v = indexed id, as the drivers' functors record them).
+// Simplex output: int64 count, count int64 ids, count float32 values.
+#include <mpi.h>
+
+#include "graph.h"
+#include "point.h"
+#include "search.h"
+#include "simplex.h"
+#include "utils.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+// Same arithmetic as the drivers' L2Distance<float> (drivers/systolic.cpp:253-269).
+template <class Atom>
+struct HarnessL2 {
+    Real operator()(const Point<Atom>& p, const Point<Atom>& q) const
+    {
+        Index dim = p.size();
+        assert((dim == q.size()));
+        Real val = 0;
+        for (Index i = 0; i < dim; ++i) {
+            Real delta = static_cast<Real>(p[i] - q[i]);
+            val += delta * delta;
+        }
+        return std::sqrt(val);
+    }
+};
+
+// Same recurrence as the drivers' EditDistance<char> (drivers/systolic.cpp:271-299).
+template <class Atom>
+struct HarnessEdit {
+    Real operator()(const Point<Atom>& s, const Point<Atom>& t) const
+    {
+        Index m = s.size(), n = t.size();
+        IndexVector v0(n + 1), v1(n + 1);
+        for (Index i = 0; i <= n; ++i) v0[i] = i;
+        for (Index i = 0; i < m; ++i) {
+            v1[0] = i + 1;
+            for (Index j = 0; j < n; ++j) {
+                Index del = v0[j + 1] + 1;
+                Index ins = v1[j] + 1;
+                Index sub = (s[i] == t[j]) ? v0[j] : v0[j] + 1;
+                v1[j + 1] = std::min(del, std::min(ins, sub));
+            }
+            std::swap(v0, v1);
+        }
+        return static_cast<Real>(v0[n]);
+    }
+};
+
+struct EdgeDump {
+    std::vector<int64_t> u, v;
+    std::vector<float> w;
+    void write(const char* path) const
+    {
+        FILE* f = std::fopen(path, "wb");
+        if (!f) { std::perror(path); std::exit(2); }
+        int64_t n = (int64_t)u.size();
+        std::fwrite(&n, sizeof(n), 1, f);
+        std::fwrite(u.data(), sizeof(int64_t), u.size(), f);
+        std::fwrite(v.data(), sizeof(int64_t), v.size(), f);
+        std::fwrite(w.data(), sizeof(float), w.size(), f);
+        std::fclose(f);
+    }
+};
+
+static int run_systolic(const char* in, Real radius, const char* out)
+{
+    MPI_Comm comm = MPI_COMM_WORLD;
+    PointContainer<float> points;
+    points.read_fvecs(in, comm);
+    HarnessL2<float> distance;
+    CoverTree tree(1.5, 10);
+    tree.build(points, distance);
+    EdgeDump dump;
+    auto functor = [&](const Point<float>& p, const Point<float>& q, Real dist) {
+        dump.u.push_back(q.id());
+        dump.v.push_back(p.id());
+        dump.w.push_back(dist);
+    };
+    PointContainer<float> queries = points;
+    for (Index i = 0; i < queries.num_points(); ++i) tree.radius_query(points, distance, queries[i], radius, functor);
+    dump.write(out);
+    return 0;
+}
+
+template <class Atom, class Distance>
+static int run_landmark(const char* in, Real radius, Index m, int seed, const char* out)
+{
+    MPI_Comm comm = MPI_COMM_WORLD;
+    PointContainer<Atom> points;
+    Index n;
+    if constexpr (std::is_same_v<Atom, char>) n = points.read_seqs(in, comm);
+    else n = points.read_fvecs(in, comm);
+    assert((m <= n));
+    IndexVector landmarks;
+    selection_sample(n, m, landmarks, seed);
+    PointContainer<Atom> mycenters, centers;
+    mycenters.indexed_gather(points, landmarks);
+    centers.allgather(mycenters, comm);
+    Distance distance;
+    VoronoiDiagram<Atom> diagram(points, centers, distance);
+    std::vector<VoronoiCell<Atom>> cells;
+    diagram.coalesce_cells(cells, comm);
+    diagram.add_ghost_points_systolic(cells, distance, radius, 1.5, 10, comm);
+    EdgeDump dump;
+    auto functor = [&](const Point<Atom>& p, const Point<Atom>& q, Real dist) {
+        dump.u.push_back(q.id());
+        dump.v.push_back(p.id());
+        dump.w.push_back(dist);
+    };
+    for (const VoronoiCell<Atom>& cell : cells) {
+        CoverTree tree(1.5, 10);
+        tree.build(cell, distance);
+        tree.radius_query_batched(cell, distance, cell, radius, functor);
+        tree.radius_query_batched(cell, distance, cell.ghosts(), radius, functor);
+    }
+    dump.write(out);
+    return 0;
+}
+
+static int run_rips(const char* in, Real radius, Index maxdim, Index m, int seed, const char* out)
+{
+    MPI_Comm comm = MPI_COMM_WORLD;
+    PointContainer<float> points;
+    Index n = points.read_fvecs(in, comm);
+    IndexVector landmarks;
+    selection_sample(n, m, landmarks, seed);
+    PointContainer<float> mycenters, centers;
+    mycenters.indexed_gather(points, landmarks);
+    centers.allgather(mycenters, comm);
+    HarnessL2<float> distance;
+    VoronoiDiagram<float> diagram(points, centers, distance);
+    std::vector<VoronoiCell<float>> cells;
+    diagram.coalesce_cells(cells, comm);
+    diagram.add_ghost_points_systolic_rips(cells, distance, radius, 1.5, 10, comm);
+    std::vector<int64_t> ids;
+    std::vector<float> values;
+    for (const VoronoiCell<float>& cell : cells) {
+        VoronoiComplex<float> vc(cell, radius, maxdim);
+        vc.build_filtration(distance, n, 1.5, 10);
+        for (auto it = vc.begin(); it != vc.end(); ++it) {
+            ids.push_back(it->getid());
+            values.push_back(it->getvalue());
+        }
+    }
+    FILE* f = std::fopen(out, "wb");
+    if (!f) { std::perror(out); return 2; }
+    int64_t cnt = (int64_t)ids.size();
+    std::fwrite(&cnt, sizeof(cnt), 1, f);
+    std::fwrite(ids.data(), sizeof(int64_t), ids.size(), f);
+    std::fwrite(values.data(), sizeof(float), values.size(), f);
+    std::fclose(f);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    MPI_Init(&argc, &argv);
+    int rc = 1;
+    if (argc == 5 && !std::strcmp(argv[1], "systolic")) {
+        rc = run_systolic(argv[2], (Real)std::atof(argv[3]), argv[4]);
+    } else if (argc == 8 && !std::strcmp(argv[1], "landmark")) {
+        Real r = (Real)std::atof(argv[4]);
+        Index m = std::atoll(argv[5]);
+        int seed = std::atoi(argv[6]);
+        if (!std::strcmp(argv[2], "edit")) rc = run_landmark<char, HarnessEdit<char>>(argv[3], r, m, seed, argv[7]);
+        else rc = run_landmark<float, HarnessL2<float>>(argv[3], r, m, seed, argv[7]);
+    } else if (argc == 8 && !std::strcmp(argv[1], "rips")) {
+        rc = run_rips(argv[2], (Real)std::atof(argv[3]), std::atoll(argv[4]), std::atoll(argv[5]), std::atoi(argv[6]),
+                      argv[7]);
+    } else {
+        std::fprintf(stderr,
+                     "usage: %s systolic <in.fvecs> <radius> <out>\n"
+                     "       %s landmark <l2|edit> <in> <radius> <m> <seed> <out>\n"
+                     "       %s rips <in.fvecs> <radius> <maxdim> <m> <seed> <out>\n",
+                     argv[0], argv[0], argv[0]);
+    }
+    MPI_Finalize();
+    return rc;
+}

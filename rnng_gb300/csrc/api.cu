@@ -1,0 +1,309 @@
+// C ABI of librnng_gpu.so (declared in include/rnng_gpu.h).  Every entry point
+// validates its arguments, runs on the context's stream, converts exceptions into
+// status codes and records the message for rnng_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "common.cuh"
+#include "eps_l2.cuh"
+#include "kernels_misc.cuh"
+
+using namespace rnng;
+
+namespace {
+
+template <class F>
+int guarded(rnng_ctx* ctx, F&& body)
+{
+    if (!ctx) return RNNG_ERR_INVALID;
+    try {
+        RNNG_CUDA(cudaSetDevice(ctx->device));
+        body();
+        ctx->last_error.clear();
+        return RNNG_OK;
+    } catch (const Error& e) {
+        ctx->last_error = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        ctx->last_error = "host allocation failed";
+        return RNNG_ERR_NOMEM;
+    } catch (...) {
+        ctx->last_error = "unknown error";
+        return RNNG_ERR_INVALID;
+    }
+}
+
+float elapsed(rnng_ctx* c, int a, int b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) return 0.f;
+    return ms;
+}
+
+void* stage(rnng_ctx* c, DevBuf& slot, size_t bytes)
+{
+    // DevBuf is reused here for a pinned host block: ptr from cudaMallocHost.
+    if (bytes <= slot.bytes) return slot.ptr;
+    if (slot.ptr) cudaFreeHost(slot.ptr);
+    slot.ptr = nullptr;
+    slot.bytes = 0;
+    size_t grow = bytes + bytes / 4 + 256;
+    RNNG_CUDA(cudaMallocHost(&slot.ptr, grow));
+    slot.bytes = grow;
+    return slot.ptr;
+}
+
+const float* upload_f32(rnng_ctx* c, DevBuf& buf, const float* X, int64_t count, unsigned flags)
+{
+    if (flags & RNNG_INPUT_DEVICE) return X;
+    buf.reserve(sizeof(float) * (size_t)std::max<int64_t>(count, 1));
+    if (count) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, X, sizeof(float) * count, cudaMemcpyHostToDevice, c->stream));
+    return buf.as<float>();
+}
+
+const int64_t* upload_i64(rnng_ctx* c, DevBuf& buf, const int64_t* v, int64_t count, unsigned flags)
+{
+    if (!v) return nullptr;
+    if (flags & RNNG_INPUT_DEVICE) return v;
+    buf.reserve(sizeof(int64_t) * (size_t)std::max<int64_t>(count, 1));
+    if (count) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, v, sizeof(int64_t) * count, cudaMemcpyHostToDevice, c->stream));
+    return buf.as<int64_t>();
+}
+
+// Hands the device edge arrays (u, v, w of length m) to the caller, either as new
+// device allocations or copied into the pinned staging area.
+void deliver_edges(rnng_ctx* c, const int64_t* du, const int64_t* dv, const float* dw, int64_t m, unsigned flags,
+                   rnng_edges* out)
+{
+    std::memset(out, 0, sizeof(*out));
+    out->count = m;
+    size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1), bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
+    if (flags & RNNG_OUTPUT_DEVICE) {
+        out->on_device = 1;
+        RNNG_CUDA(cudaMalloc(&out->u, bi));
+        RNNG_CUDA(cudaMalloc(&out->v, bi));
+        RNNG_CUDA(cudaMalloc(&out->w, bf));
+        if (m) {
+            RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, c->stream));
+            RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, c->stream));
+            RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToDevice, c->stream));
+        }
+    } else {
+        out->staged = 1;
+        char* h = (char*)stage(c, c->host_stage, 2 * bi + bf);
+        out->u = (int64_t*)h;
+        out->v = (int64_t*)(h + bi);
+        out->w = (float*)(h + 2 * bi);
+        if (m) {
+            RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
+            RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
+            RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream));
+        }
+    }
+}
+
+// Runs the tile stage, growing the edge buffer and re-running when it overflowed.
+int64_t tiles_with_retry(rnng_ctx* c, Layout& L, int mode, EdgeOut& E)
+{
+    unsigned long long cap = std::max<unsigned long long>(1u << 20, c->edge_cap_hint);
+    c->counters.reserve(sizeof(unsigned long long) * 8);
+    E.count = c->counters.as<unsigned long long>() + 4;
+    for (int attempt = 0;; ++attempt) {
+        c->edges_u.reserve(sizeof(uint32_t) * cap);
+        c->edges_v.reserve(sizeof(uint32_t) * cap);
+        c->edges_w.reserve(sizeof(float) * cap);
+        E.si = c->edges_u.as<uint32_t>();
+        E.sj = c->edges_v.as<uint32_t>();
+        E.w = c->edges_w.as<float>();
+        E.cap = cap;
+        RNNG_CUDA(cudaMemsetAsync(E.count, 0, sizeof(unsigned long long), c->stream));
+        if (mode == RNNG_MODE_BF16_RECHECK) run_tiles_bf16(c, L, E);
+        else run_tiles_fp32(c, L, E);
+        unsigned long long got = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&got, E.count, sizeof(got), cudaMemcpyDeviceToHost, c->stream));
+        RNNG_CUDA(cudaStreamSynchronize(c->stream));
+        check_device_fault(c);
+        if (got <= cap) {
+            c->edge_cap_hint = std::max<unsigned long long>(c->edge_cap_hint, got + got / 8);
+            return (int64_t)got;
+        }
+        RNNG_REQUIRE(attempt < 2, RNNG_ERR_OVERFLOW, "edge buffer overflow after regrowth");
+        cap = got + got / 8 + 1024;
+        c->stats.retries++;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rnng_ctx_create(int device, rnng_ctx** out)
+{
+    if (!out) return RNNG_ERR_INVALID;
+    *out = nullptr;
+    rnng_ctx* c = new (std::nothrow) rnng_ctx;
+    if (!c) return RNNG_ERR_NOMEM;
+    c->device = device;
+    int rc = guarded(c, [&] {
+        int ndev = 0;
+        RNNG_CUDA(cudaGetDeviceCount(&ndev));
+        RNNG_REQUIRE(device >= 0 && device < ndev, RNNG_ERR_INVALID, "no such device");
+        RNNG_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        RNNG_CUDA(cudaGetDeviceProperties(&prop, device));
+        RNNG_REQUIRE(prop.major >= 10, RNNG_ERR_UNSUPPORTED, "librnng_gpu needs a Blackwell (sm_100 family) GPU");
+        c->num_sms = prop.multiProcessorCount;
+        RNNG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+        ensure_events(c);
+        init_device_fault(c);
+    });
+    if (rc != RNNG_OK) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return RNNG_OK;
+}
+
+int rnng_ctx_destroy(rnng_ctx* c)
+{
+    if (!c) return RNNG_ERR_INVALID;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    rnng_ctx_trim(c);
+    if (c->have_events)
+        for (auto& e : c->ev) cudaEventDestroy(e);
+    if (c->fault_word) cudaFree(c->fault_word);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RNNG_OK;
+}
+
+const char* rnng_last_error(const rnng_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+
+int rnng_get_stats(const rnng_ctx* c, rnng_stats* out)
+{
+    if (!c || !out) return RNNG_ERR_INVALID;
+    *out = c->stats;
+    return RNNG_OK;
+}
+
+int rnng_ctx_stream(rnng_ctx* c, void** stream)
+{
+    if (!c || !stream) return RNNG_ERR_INVALID;
+    *stream = (void*)c->stream;
+    return RNNG_OK;
+}
+
+int rnng_ctx_trim(rnng_ctx* c)
+{
+    if (!c) return RNNG_ERR_INVALID;
+    return guarded(c, [&] {
+        RNNG_CUDA(cudaStreamSynchronize(c->stream));
+        DevBuf* bufs[] = {&c->x_in, &c->ids_in, &c->x_sorted, &c->xb_sorted, &c->norms, &c->perm, &c->keys,
+                          &c->keys_alt, &c->perm_alt, &c->cell, &c->dist, &c->pivots, &c->tile_lo, &c->tile_hi,
+                          &c->super_lo, &c->super_hi, &c->pair_list, &c->super_list, &c->counters, &c->edges_u,
+                          &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
+                          &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7};
+        for (DevBuf* b : bufs) b->release();
+        if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
+        c->host_stage.ptr = nullptr;
+        c->host_stage.bytes = 0;
+        c->edge_cap_hint = 0;
+    });
+}
+
+int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius, int mode,
+                      unsigned flags, rnng_edges* out)
+{
+    if (!c) return RNNG_ERR_INVALID;
+    return guarded(c, [&] {
+        RNNG_REQUIRE(out != nullptr, RNNG_ERR_INVALID, "out is null");
+        std::memset(out, 0, sizeof(*out));
+        RNNG_REQUIRE(n >= 0 && d >= 1 && (n == 0 || X != nullptr), RNNG_ERR_INVALID, "bad points");
+        RNNG_REQUIRE(n < (int64_t(1) << 31) - kTile, RNNG_ERR_INVALID, "n too large (int32 point indices)");
+        RNNG_REQUIRE(d <= 65536, RNNG_ERR_INVALID, "d too large");
+        RNNG_REQUIRE(mode == RNNG_MODE_FP32_DIRECT || mode == RNNG_MODE_BF16_RECHECK, RNNG_ERR_INVALID, "bad mode");
+        RNNG_REQUIRE(!(radius != radius), RNNG_ERR_INVALID, "radius is NaN");
+        if (mode == RNNG_MODE_BF16_RECHECK)
+            RNNG_REQUIRE(bf16_supported((int)d), RNNG_ERR_UNSUPPORTED, "BF16 mode needs d % 8 == 0 and d <= 1024");
+        c->stats = rnng_stats{};
+        cudaStream_t s = c->stream;
+        RNNG_CUDA(cudaEventRecord(c->ev[0], s));
+        const float* dX = upload_f32(c, c->x_in, X, n * d, flags);
+        const int64_t* dids = upload_i64(c, c->ids_in, ids, n, flags);
+        RNNG_CUDA(cudaEventRecord(c->ev[1], s));
+        if (n < 2 || radius < 0.f) {
+            // no pair can be an edge (a negative radius admits no distance)
+            RNNG_CUDA(cudaEventRecord(c->ev[2], s));
+            deliver_edges(c, nullptr, nullptr, nullptr, 0, flags, out);
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            return;
+        }
+        Layout L = build_layout(c, dX, n, (int)d, radius);
+        RNNG_CUDA(cudaEventRecord(c->ev[2], s));
+        compute_bounds(c, L);
+        RNNG_CUDA(cudaEventRecord(c->ev[3], s));
+        prune(c, L);
+        RNNG_CUDA(cudaEventRecord(c->ev[4], s));
+        if (mode == RNNG_MODE_BF16_RECHECK) prepare_bf16(c, L);
+        EdgeOut E;
+        int64_t m = tiles_with_retry(c, L, mode, E);
+        RNNG_CUDA(cudaEventRecord(c->ev[5], s));
+        c->out_u.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
+        c->out_v.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
+        c->out_w.reserve(sizeof(float) * std::max<int64_t>(m, 1));
+        finalize_edges(c, L, dids, E, m, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>());
+        if (flags & RNNG_SORT_OUTPUT)
+            sort_edges_uv(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m);
+        RNNG_CUDA(cudaEventRecord(c->ev[6], s));
+        deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m, flags, out);
+        RNNG_CUDA(cudaEventRecord(c->ev[7], s));
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        RNNG_CUDA(cudaGetLastError());
+        rnng_stats& st = c->stats;
+        st.ms_h2d = elapsed(c, 0, 1);
+        st.ms_partition = elapsed(c, 1, 2);
+        st.ms_bounds = elapsed(c, 2, 3);
+        st.ms_prune = elapsed(c, 3, 4);
+        st.ms_tiles = elapsed(c, 4, 5);
+        st.ms_finalize = elapsed(c, 5, 6);
+        st.ms_d2h = elapsed(c, 6, 7);
+        st.ms_total = elapsed(c, 0, 7);
+        st.num_cells = L.num_cells;
+        st.tile_pairs = (int64_t)L.tile_pairs;
+        st.tile_pairs_all = L.T * (L.T + 1) / 2;
+        st.pairs_evaluated = (int64_t)L.tile_pairs * kTile * kTile;
+        st.edges = m;
+        st.candidates = c->last_candidates;
+    });
+}
+
+int rnng_edges_free(rnng_edges* e)
+{
+    if (!e) return RNNG_ERR_INVALID;
+    if (e->on_device) {
+        cudaFree(e->u);
+        cudaFree(e->v);
+        cudaFree(e->w);
+    }
+    std::memset(e, 0, sizeof(*e));
+    return RNNG_OK;
+}
+
+int rnng_simplices_free(rnng_simplices* s)
+{
+    if (!s) return RNNG_ERR_INVALID;
+    if (s->on_device) {
+        cudaFree(s->id);
+        cudaFree(s->value);
+    }
+    std::memset(s, 0, sizeof(*s));
+    return RNNG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+// Shared definitions for the RNNG GB300 library: status codes, the context, the
+// device scratch arena and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/rnng_gpu.h"
+
+namespace rnng {
+
+// Raised inside the library and turned into a status code at the C boundary.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+#define RNNG_CUDA(call)                                                                                  \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) {                                                                         \
+            throw ::rnng::Error{RNNG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                                                   __FILE__ + ":" + std::to_string(__LINE__) + ")"};     \
+        }                                                                                                \
+    } while (0)
+
+#define RNNG_REQUIRE(cond, code, text)                 \
+    do {                                               \
+        if (!(cond)) throw ::rnng::Error{(code), (text)}; \
+    } while (0)
+
+// A growable device buffer owned by the context.  Buffers are reused across calls
+// so that steady-state calls do not allocate.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    void reserve(size_t want)
+    {
+        if (want <= bytes) return;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t grow = want + want / 4 + 256;
+        RNNG_CUDA(cudaMalloc(&ptr, grow));
+        bytes = grow;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const { return reinterpret_cast<T*>(ptr); }
+};
+
+// Device-side error word: kernels with bounded waits record a code here instead
+// of spinning forever; the host checks it after the stage.
+enum DeviceFault : int {
+    FAULT_NONE = 0,
+    FAULT_MBAR_TIMEOUT = 1,
+    FAULT_QUEUE = 2,
+};
+
+}  // namespace rnng
+
+// The context: one device, one stream, reusable scratch, last-call statistics.
+struct rnng_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string last_error;
+    rnng_stats stats{};
+    // named scratch buffers
+    rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
+        tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
+        out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7;
+    rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
+    unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;
+    int64_t last_candidates = 0;
+    // BF16 Gram operands of the current call: TMA descriptor (a CUtensorMap), padded
+    // dimension, per-row candidate-test data and the widened radius
+    alignas(64) unsigned char tmap[128] = {};
+    int bf16_dp = 0;
+    void* bf16_rowinfo = nullptr;
+    float bf16_eps_p = 0.f;
+    int* fault_word = nullptr;  // device error word written by kernels with bounded waits
+    cudaEvent_t ev[16] = {};
+    bool have_events = false;
+};
+
+namespace rnng {
+
+inline void ensure_events(rnng_ctx* c)
+{
+    if (c->have_events) return;
+    for (auto& e : c->ev) RNNG_CUDA(cudaEventCreate(&e));
+    c->have_events = true;
+}
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Reference L2 (drivers/systolic.cpp:253-269): sequential difference-square-sum in
+// float without contraction, then a correctly rounded square root.  The explicit
+// _rn intrinsics are never fused into FMA by the compiler.
+__device__ __forceinline__ float l2seq_acc(float acc, float a, float b)
+{
+    float d = __fsub_rn(a, b);
+    return __fadd_rn(acc, __fmul_rn(d, d));
+}
+
+}  // namespace rnng

@@ -1,0 +1,69 @@
+// Device fault word and edge sorting shared by the pipelines.
+#include <cub/cub.cuh>
+
+#include "kernels_misc.cuh"
+
+namespace rnng {
+
+void init_device_fault(rnng_ctx* c)
+{
+    if (!c->fault_word) RNNG_CUDA(cudaMalloc(&c->fault_word, sizeof(int) * 4));
+    RNNG_CUDA(cudaMemset(c->fault_word, 0, sizeof(int) * 4));
+}
+
+void check_device_fault(rnng_ctx* c)
+{
+    int h[4] = {0, 0, 0, 0};
+    RNNG_CUDA(cudaMemcpyAsync(h, c->fault_word, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    RNNG_CUDA(cudaStreamSynchronize(c->stream));
+    if (h[0] != FAULT_NONE) {
+        RNNG_CUDA(cudaMemsetAsync(c->fault_word, 0, sizeof(int) * 4, c->stream));
+        throw Error{RNNG_ERR_DEVICE, "kernel fault word " + std::to_string(h[0]) + " (detail " + std::to_string(h[1]) +
+                                         ", " + std::to_string(h[2]) + ")"};
+    }
+}
+
+__global__ void k_iota(int32_t* out, int64_t m)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (int32_t)i;
+}
+
+template <class T>
+__global__ void k_gather(const T* __restrict__ src, const int32_t* __restrict__ idx, T* __restrict__ dst, int64_t m)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[idx[i]];
+}
+
+void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m)
+{
+    if (m <= 1) return;
+    RNNG_REQUIRE(m < (int64_t(1) << 31), RNNG_ERR_INVALID, "too many edges to sort");
+    cudaStream_t s = c->stream;
+    c->aux6.reserve(sizeof(int64_t) * 2 * m);
+    c->aux7.reserve(sizeof(int32_t) * 2 * m + sizeof(float) * m);
+    int64_t* kbuf = c->aux6.as<int64_t>();
+    int32_t* i0 = c->aux7.as<int32_t>();
+    int32_t* i1 = i0 + m;
+    float* wtmp = (float*)(i1 + m);
+    int grid = (int)std::min<int64_t>((m + 255) / 256, (int64_t)c->num_sms * 8);
+    k_iota<<<grid, 256, 0, s>>>(i0, m);
+    size_t tmp = 0;
+    // pass 1: by v (stable), pass 2: by u (stable) -> ordered by (u, v)
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s));
+    c->cub_tmp.reserve(tmp);
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s));
+    k_gather<int64_t><<<grid, 256, 0, s>>>(u, i1, kbuf + m, m);
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
+    c->cub_tmp.reserve(tmp);
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
+    // i0 = final order; u sorted = kbuf; v and w gathered
+    RNNG_CUDA(cudaMemcpyAsync(u, kbuf, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
+    k_gather<int64_t><<<grid, 256, 0, s>>>(v, i0, kbuf, m);
+    RNNG_CUDA(cudaMemcpyAsync(v, kbuf, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
+    k_gather<float><<<grid, 256, 0, s>>>(w, i0, wtmp, m);
+    RNNG_CUDA(cudaMemcpyAsync(w, wtmp, sizeof(float) * m, cudaMemcpyDeviceToDevice, s));
+}
+
+}  // namespace rnng

@@ -1,0 +1,97 @@
+"""GPU L2 epsilon graph (both tile modes) against the CPU oracle and the golden
+fixtures made by RNNG's own code.  Bar: bit-exact edge sets and weights."""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_points
+
+pytestmark = pytest.mark.gpu
+MODES = ["fp32", "bf16"]
+
+
+def same(a, b):
+    (u1, v1, w1), (u2, v2, w2) = a, b
+    return (np.array_equal(u1, u2) and np.array_equal(v1, v2)
+            and np.array_equal(np.asarray(w1, np.float32).view(np.uint32), np.asarray(w2, np.float32).view(np.uint32)))
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name", ["k1_systolic", "k2_landmark", "k5_landmark"])
+def test_golden_fixture(ctx, mode, name):
+    g = golden(name)
+    got = ctx.eps_graph_l2(golden_points(g), g["radius"], mode=mode)
+    assert same(got, (g["u"], g["v"], g["w"]))
+
+
+CASES = [
+    # (n, d, scale, radius, seed)
+    (2, 3, 1.0, 10.0, 0),
+    (127, 5, 1.0, 1.0, 1),
+    (129, 16, 1.0, 3.0, 2),
+    (300, 64, 1.0, 9.0, 3),
+    (1000, 33, 0.5, 3.0, 4),
+    (2000, 128, 1.0, 14.5, 5),
+    (777, 200, 1.0, 18.0, 6),
+    (3000, 8, 3.0, 1.2, 7),
+]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("case", CASES)
+def test_random_against_oracle(ctx, orc, mode, case):
+    n, d, scale, r, seed = case
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10, 10, size=(8, d))
+    x = (centres[rng.integers(0, 8, n)] + scale * rng.normal(size=(n, d))).astype(np.float32)
+    want = orc.eps_graph_l2(x, np.float32(r))
+    got = ctx.eps_graph_l2(x, np.float32(r), mode=mode)
+    assert same(got, want), (len(got[0]), len(want[0]))
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_edge_cases(ctx, orc, mode):
+    # empty and single point
+    for n in (0, 1):
+        u, v, w = ctx.eps_graph_l2(np.zeros((n, 4), np.float32), 1.0, mode=mode)
+        assert u.size == 0
+    # duplicates: every pair is an edge at distance 0, also with radius 0
+    x = np.ones((300, 12), np.float32)
+    for r in (0.0, 0.5):
+        u, v, w = ctx.eps_graph_l2(x, r, mode=mode)
+        assert u.size == 300 * 299 // 2 and np.all(w == 0)
+    # negative radius admits nothing
+    u, v, w = ctx.eps_graph_l2(x, -1.0, mode=mode)
+    assert u.size == 0
+    # radius exactly at a realised distance is included (<=)
+    rng = np.random.default_rng(9)
+    y = rng.normal(size=(500, 7)).astype(np.float32)
+    ou, ov, ow = orc.eps_graph_l2(y, np.float32(1.0))
+    r = ow[len(ow) // 2]
+    assert same(ctx.eps_graph_l2(y, r, mode=mode), orc.eps_graph_l2(y, r))
+    # explicit ids: edges are reported in id space with u < v
+    ids = (np.arange(500, dtype=np.int64)[::-1] * 3 + 11).copy()
+    gu, gv, gw = ctx.eps_graph_l2(y, r, mode=mode, ids=ids)
+    wu, wv = ids[ou[ow <= r]], ids[ov[ow <= r]]
+    a, b = np.minimum(wu, wv), np.maximum(wu, wv)
+    order = np.lexsort((b, a))
+    assert np.array_equal(gu, a[order]) and np.array_equal(gv, b[order])
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_integer_descriptors_30k(ctx, orc, mode):
+    from rnng_gb300 import synth
+    x = synth.descriptor(n=30000, d=128, k=30, seed=12)
+    r = synth.EPS_K2
+    assert same(ctx.eps_graph_l2(x, r, mode=mode), orc.eps_graph_l2(x, r))
+
+
+def test_modes_agree_and_fp64_error(ctx):
+    from rnng_gb300 import synth
+    x = synth.zipf_mixture(n=40000, d=32, k=256, seed=21)
+    r = np.float32(3.0)
+    a = ctx.eps_graph_l2(x, r, mode="fp32")
+    b = ctx.eps_graph_l2(x, r, mode="bf16")
+    assert same(a, b) and a[0].size > 0
+    u, v, w = a
+    d64 = np.sqrt(((x[u].astype(np.float64) - x[v].astype(np.float64)) ** 2).sum(1))
+    assert np.max(np.abs(w - d64)) < 1e-5 * max(1.0, float(r))

@@ -1,0 +1,117 @@
+"""The CPU oracle pinned against RNNG's own outputs (golden fixtures made by running
+RNNG's headers, tests/golden/make_golden.py) and against hand-checked known answers."""
+import itertools
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, golden_points
+
+EDGE_FIXTURES = ["k1_systolic", "k1_landmark", "k2_landmark", "k5_landmark"]
+
+
+@pytest.mark.parametrize("name", EDGE_FIXTURES)
+def test_oracle_l2_matches_reference(orc, name):
+    g = golden(name)
+    x = golden_points(g)
+    u, v, w = orc.eps_graph_l2(x, g["radius"])
+    assert np.array_equal(u, g["u"]) and np.array_equal(v, g["v"])
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    # the driver's printed count is n + 2|E| (self-loops and both orientations)
+    assert int(g["reported_edges"]) == int(g["n"]) + 2 * u.size
+
+
+def test_oracle_edit_matches_reference(orc):
+    g = golden("k3_edit")
+    u, v, w = orc.eps_graph_edit(g["atoms"], g["offsets"], g["radius"])
+    assert np.array_equal(u, g["u"]) and np.array_equal(v, g["v"])
+    assert np.array_equal(w, g["w"])
+    assert int(g["reported_edges"]) == int(g["n"]) + 2 * u.size
+
+
+def test_oracle_rips_matches_reference(orc):
+    g = golden("k4_rips")
+    u, v, w = orc.eps_graph_l2(g["x"], g["radius"])
+    ids, vals = orc.rips(int(g["n"]), u, v, w, int(g["maxdim"]))
+    assert np.array_equal(ids, g["ids"])
+    assert np.array_equal(vals.view(np.uint32), g["values"].view(np.uint32))
+
+
+def _lev(s, t):
+    prev = list(range(len(t) + 1))
+    for i, a in enumerate(s, 1):
+        cur = [i]
+        for j, b in enumerate(t, 1):
+            cur.append(min(prev[j] + 1, cur[j - 1] + 1, prev[j - 1] + (a != b)))
+        prev = cur
+    return prev[-1]
+
+
+def test_edit_known_answers(orc):
+    cases = [(b"kitten", b"sitting", 3), (b"", b"abc", 3), (b"abc", b"", 3), (b"", b"", 0), (b"abc", b"abc", 0),
+             (b"flaw", b"lawn", 2), (b"ACGT", b"TGCA", 4), (b"AAAA", b"AAA", 1)]
+    for s, t, want in cases:
+        assert orc.edit(s, t) == want
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        s = bytes(rng.choice(list(b"ACGT"), size=rng.integers(0, 40)))
+        t = bytes(rng.choice(list(b"ACGT"), size=rng.integers(0, 40)))
+        assert orc.edit(s, t) == _lev(s, t) == orc.edit(t, s)
+
+
+def test_l2seq_is_sequential_float32(orc):
+    rng = np.random.default_rng(1)
+    for d in (1, 3, 8, 31, 128, 200):
+        p = rng.normal(size=d).astype(np.float32) * 7
+        q = rng.normal(size=d).astype(np.float32) * 7
+        acc = np.float32(0)
+        for k in range(d):
+            delta = np.float32(p[k] - q[k])
+            acc = np.float32(acc + np.float32(delta * delta))
+        assert orc.l2seq(p, q) == np.sqrt(acc, dtype=np.float32)
+        assert orc.l2seq(p, q) == orc.l2seq(q, p)
+
+
+def test_binom_and_simplex_ids(orc):
+    assert orc.binom(5, 2) == 10 and orc.binom(0, 1) == 0 and orc.binom(1, 2) == 0 and orc.binom(7, 0) == 1
+    assert orc.binom(500000, 3) == 500000 * 499999 * 499998 // 6
+    assert orc.simplex_id([3]) == 3
+    assert orc.simplex_id([4, 1]) == (1 + 6) | (1 << 60)
+    assert orc.simplex_id([0, 2, 5]) == (0 + 1 + 10) | (2 << 60)
+
+
+def test_rips_against_brute_force(orc):
+    rng = np.random.default_rng(2)
+    n = 40
+    x = rng.normal(size=(n, 3)).astype(np.float32)
+    r = np.float32(1.2)
+    u, v, w = orc.eps_graph_l2(x, r)
+    wmap = {(a, b): c for a, b, c in zip(u.tolist(), v.tolist(), w.tolist())}
+    want = [(0.0, orc.simplex_id([i])) for i in range(n)]
+    want += [(c, orc.simplex_id([a, b])) for (a, b), c in wmap.items()]
+    for a, b, c in itertools.combinations(range(n), 3):
+        if (a, b) in wmap and (a, c) in wmap and (b, c) in wmap:
+            want.append((max(wmap[(a, b)], wmap[(a, c)], wmap[(b, c)]), orc.simplex_id([a, b, c])))
+    want.sort()
+    ids, vals = orc.rips(n, u, v, w, 2)
+    assert [int(i) for i in ids] == [i for _, i in want]
+    assert np.array_equal(vals, np.array([val for val, _ in want], np.float32))
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="needs the RNNG sources to build its drivers")
+def test_unchanged_reference_drivers_agree(orc, tmp_path):
+    """RNNG's own drivers, built unchanged against the MPI shim, report the fixture's counts."""
+    orc.build(ref=True)
+    g = golden("k1_systolic")
+    from rnng_gb300 import synth
+    p = str(tmp_path / "k1.fvecs")
+    synth.write_fvecs(p, g["x"])
+    for drv, extra in (("systolic", []), ("landmark", ["-m", "30", "-F", "-s", "7"])):
+        out = str(tmp_path / f"{drv}.mtx")
+        r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", drv), "-i", p, "-r", "1.5", "-o", out] + extra,
+                           capture_output=True, text=True, check=True)
+        assert f"edges={int(g['reported_edges'])}" in r.stderr
+        lines = open(out).read().split("\n")
+        assert lines[0].split()[-1] == str(int(g["reported_edges"]))

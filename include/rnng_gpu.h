@@ -78,8 +78,9 @@ typedef struct rnng_simplices {
 
 /* Counters and stage times of the last call on a context (milliseconds). */
 typedef struct rnng_stats {
-    double ms_total, ms_h2d, ms_partition, ms_sort, ms_bounds, ms_prune, ms_tiles, ms_finalize, ms_d2h;
+    double ms_total, ms_h2d, ms_partition, ms_sort, ms_bounds, ms_prune, ms_tiles, ms_recheck, ms_finalize, ms_d2h;
     int64_t num_cells;      /* landmarks / cells of the partition */
+    int64_t super_pairs;    /* super-tile pairs that survived the first pruning level */
     int64_t tile_pairs;     /* tile pairs that survived pruning */
     int64_t tile_pairs_all; /* tile pairs before pruning */
     int64_t pairs_evaluated;/* point pairs inside surviving tiles */

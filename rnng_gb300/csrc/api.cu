@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "eps_l2.cuh"
+#include "balls.cuh"
 #include "kernels_misc.cuh"
 
 using namespace rnng;
@@ -208,7 +209,7 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->keys_alt, &c->perm_alt, &c->cell, &c->dist, &c->pivots, &c->tile_lo, &c->tile_hi,
                           &c->super_lo, &c->super_hi, &c->pair_list, &c->super_list, &c->counters, &c->edges_u,
                           &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
-                          &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7};
+                          &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;
@@ -230,7 +231,7 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         RNNG_REQUIRE(mode == RNNG_MODE_FP32_DIRECT || mode == RNNG_MODE_BF16_RECHECK, RNNG_ERR_INVALID, "bad mode");
         RNNG_REQUIRE(!(radius != radius), RNNG_ERR_INVALID, "radius is NaN");
         if (mode == RNNG_MODE_BF16_RECHECK)
-            RNNG_REQUIRE(bf16_supported((int)d), RNNG_ERR_UNSUPPORTED, "BF16 mode needs d % 8 == 0 and d <= 1024");
+            RNNG_REQUIRE(bf16_supported((int)d), RNNG_ERR_UNSUPPORTED, "BF16 mode supports d <= 256");
         c->stats = rnng_stats{};
         cudaStream_t s = c->stream;
         RNNG_CUDA(cudaEventRecord(c->ev[0], s));
@@ -246,11 +247,15 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         }
         Layout L = build_layout(c, dX, n, (int)d, radius);
         RNNG_CUDA(cudaEventRecord(c->ev[2], s));
-        compute_bounds(c, L);
+        build_covers(c, L);
         RNNG_CUDA(cudaEventRecord(c->ev[3], s));
-        prune(c, L);
+        prune_covers(c, L);
         RNNG_CUDA(cudaEventRecord(c->ev[4], s));
-        if (mode == RNNG_MODE_BF16_RECHECK) prepare_bf16(c, L);
+        if (mode == RNNG_MODE_BF16_RECHECK) {
+            schedule_pairs(c, L, (int)std::max<unsigned long long>(
+                                     1, std::min<unsigned long long>(L.tile_pairs, (unsigned long long)c->num_sms)));
+            prepare_bf16(c, L);
+        }
         EdgeOut E;
         int64_t m = tiles_with_retry(c, L, mode, E);
         RNNG_CUDA(cudaEventRecord(c->ev[5], s));
@@ -270,11 +275,17 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         st.ms_partition = elapsed(c, 1, 2);
         st.ms_bounds = elapsed(c, 2, 3);
         st.ms_prune = elapsed(c, 3, 4);
-        st.ms_tiles = elapsed(c, 4, 5);
+        if (mode == RNNG_MODE_BF16_RECHECK) {
+            st.ms_tiles = elapsed(c, 4, 8);
+            st.ms_recheck = elapsed(c, 8, 5);
+        } else {
+            st.ms_tiles = elapsed(c, 4, 5);
+        }
         st.ms_finalize = elapsed(c, 5, 6);
         st.ms_d2h = elapsed(c, 6, 7);
         st.ms_total = elapsed(c, 0, 7);
         st.num_cells = L.num_cells;
+        st.super_pairs = (int64_t)L.super_pairs;
         st.tile_pairs = (int64_t)L.tile_pairs;
         st.tile_pairs_all = L.T * (L.T + 1) / 2;
         st.pairs_evaluated = (int64_t)L.tile_pairs * kTile * kTile;

@@ -1,0 +1,589 @@
+// Tile covers and exact tile-pair pruning by the triangle inequality.
+//
+// Every tile (128 consecutive points of the partition order) is covered by up to
+// kBalls balls: the tile is split by farthest-point bisection (take the group with
+// the largest radius, its point a farthest from the centroid, the point b farthest
+// from a, and move the points closer to b than to a into a new group) until it has
+// kBalls groups; each group is stored as (centroid, radius).  A super-tile (kSuper
+// consecutive tiles) gets kBalls balls built the same way from its tiles' balls.
+// A pair of tiles (or super-tiles) is skipped when every pair of their balls is
+// separated:  |c1 - c2| (1 - relerr) > eps' + r1 + r2, with radii widened by the
+// relative error of their float computation and eps' = eps * (1 + (d+8) 2^-24).
+// Then no x in ball 1 and y in ball 2 can have the reference L2 <= eps, so the
+// pruning never drops an edge.  This is RNNG's ghost-point reasoning
+// (include/point.hpp:904, d(q, c) <= d(q, c_q) + 2r) with balls instead of cells.
+//
+// Leaf order: the children of every split cell are chained greedily by their
+// landmarks (start at the first, always step to the nearest unvisited one), so
+// cells that follow each other in the order are close and tiles rarely straddle
+// far clusters.
+#include <cub/cub.cuh>
+
+#include <vector>
+
+#include "balls.cuh"
+#include "common.cuh"
+#include "eps_l2.cuh"
+#include "partition.cuh"
+
+namespace rnng {
+
+// ------------------------------------------------------------------------------------------------
+// leaf chaining
+
+constexpr int kChainMax = kFan;  // children per cell never exceed the partition fan-out
+
+__device__ __forceinline__ int tri_index(int i, int j, int m)
+{
+    if (i > j) { const int t = i; i = j; j = t; }
+    return i * m - i * (i + 1) / 2 + (j - i - 1);
+}
+
+// One block per parent cell: pairwise distances of its children's landmarks into
+// shared memory (upper triangle; a warp per pair, lanes over dimensions), then one
+// warp walks the greedy chain.
+__global__ void __launch_bounds__(256) k_chain_leaves(const float* __restrict__ L, int d,
+                                                      const int32_t* __restrict__ m2,
+                                                      const int32_t* __restrict__ m2_off, int32_t* __restrict__ rank)
+{
+    extern __shared__ float Dm[];  // m x m
+    const int c = blockIdx.x, m = m2[c], base = m2_off[c];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (m <= 0) return;
+    if (m == 1) {
+        if (threadIdx.x == 0) rank[base] = base;
+        return;
+    }
+    for (int p = warp; p < m * m; p += nw) {
+        const int i = p / m, j = p % m;
+        if (j <= i) continue;  // warp-uniform
+        const float* a = L + (int64_t)(base + i) * d;
+        const float* b = L + (int64_t)(base + j) * d;
+        float s = 0.f;
+        for (int k = lane; k < d; k += 32) {
+            const float t = a[k] - b[k];
+            s = fmaf(t, t, s);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) Dm[tri_index(i, j, m)] = s;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    // visited flags in registers: lane l owns landmarks l, l+32, ... (m <= kFan)
+    uint32_t seen = 0;
+    int cur = 0;
+    if (lane == 0) {
+        seen |= 1u;
+        rank[base] = base;
+    }
+    for (int step = 1; step < m; ++step) {
+        float best = INFINITY;
+        int bi = m;
+        for (int q = 0; q * 32 + lane < m; ++q) {
+            const int j = q * 32 + lane;
+            if ((seen >> q) & 1u) continue;
+            const float v = Dm[tri_index(cur, j, m)];
+            if (v < best || (v == best && j < bi)) { best = v; bi = j; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (bi >= m) break;
+        if ((bi & 31) == lane) seen |= 1u << (bi >> 5);
+        if (lane == 0) rank[base + bi] = base + step;
+        cur = bi;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// farthest-point bisection shared by tile balls (over points) and super balls (over balls)
+
+// Per-block workspace.  Items are rows of `src` (points, or ball centres with
+// item radii `irad`).  Dimensions are walked with a stride so d is unbounded.
+struct BisectState {
+    int label[kSuper * kBalls > kTile ? kSuper * kBalls : kTile];
+    float dist[kSuper * kBalls > kTile ? kSuper * kBalls : kTile];
+    float rad[kBalls];
+    int far_idx[kBalls];
+    int count[kBalls];
+    int ngroups;
+    int a, b;
+    float red_v[256];
+    int red_i[256];
+};
+
+// block-wide (max value, index) reduction; ties -> smaller index
+__device__ void block_argmax(BisectState& st, float v, int i, float& out_v, int& out_i)
+{
+    st.red_v[threadIdx.x] = v;
+    st.red_i[threadIdx.x] = i;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const float ov = st.red_v[threadIdx.x + o];
+            const int oi = st.red_i[threadIdx.x + o];
+            if (ov > st.red_v[threadIdx.x] || (ov == st.red_v[threadIdx.x] && oi < st.red_i[threadIdx.x])) {
+                st.red_v[threadIdx.x] = ov;
+                st.red_i[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    out_v = st.red_v[0];
+    out_i = st.red_i[0];
+    __syncthreads();
+}
+
+// Euclidean distance of item r to vector v (length d), one warp.
+__device__ __forceinline__ float warp_dist(const float* __restrict__ x, const float* __restrict__ v, int d)
+{
+    const int lane = threadIdx.x & 31;
+    float s = 0.f;
+    for (int k = lane; k < d; k += 32) {
+        const float t = x[k] - v[k];
+        s = fmaf(t, t, s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return sqrtf(s);
+}
+
+// centroid of group g into cen (d floats, global scratch owned by the block)
+__device__ void group_centroid(BisectState& st, const float* __restrict__ src, int nitems, int d, int g,
+                               float* __restrict__ cen)
+{
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        float s = 0.f;
+        int cnt = 0;
+        for (int r = 0; r < nitems; ++r)
+            if (st.label[r] == g) {
+                s += src[(int64_t)r * d + k];
+                ++cnt;
+            }
+        cen[k] = cnt ? s / (float)cnt : 0.f;
+    }
+    __syncthreads();
+}
+
+// radius of group g around cen: max over items of |x - cen| + irad (irad may be null)
+__device__ void group_radius(BisectState& st, const float* __restrict__ src, const float* __restrict__ irad,
+                             int nitems, int d, int g, const float* __restrict__ cen)
+{
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < nitems; r += nw) {
+        if (st.label[r] != g) continue;  // warp-uniform
+        const float dd = warp_dist(src + (int64_t)r * d, cen, d);
+        if ((threadIdx.x & 31) == 0) st.dist[r] = dd + (irad ? irad[r] : 0.f);
+    }
+    __syncthreads();
+    float best = -1.f;
+    int bi = -1, cnt = 0;
+    for (int r = threadIdx.x; r < nitems; r += blockDim.x)
+        if (st.label[r] == g) {
+            ++cnt;
+            if (st.dist[r] > best) { best = st.dist[r]; bi = r; }
+        }
+    float v;
+    int i;
+    block_argmax(st, best, bi, v, i);
+    // counts via a second reduction on the same buffers
+    st.red_i[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) st.red_i[threadIdx.x] += st.red_i[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st.rad[g] = v;
+        st.far_idx[g] = i;
+        st.count[g] = st.red_i[0];
+    }
+    __syncthreads();
+}
+
+// Splits items into up to kBalls groups; centres written to cen[kBalls][d].
+__device__ void bisect(BisectState& st, const float* __restrict__ src, const float* __restrict__ irad, int nitems,
+                       int d, float* __restrict__ cen)
+{
+    for (int r = threadIdx.x; r < nitems; r += blockDim.x) st.label[r] = 0;
+    if (threadIdx.x == 0) st.ngroups = 1;
+    __syncthreads();
+    group_centroid(st, src, nitems, d, 0, cen);
+    group_radius(st, src, irad, nitems, d, 0, cen);
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    while (st.ngroups < kBalls) {
+        // group with the largest radius that can still be split
+        int g = -1;
+        float gr = 0.f;
+        for (int k = 0; k < st.ngroups; ++k)
+            if (st.count[k] >= 2 && st.rad[k] > gr) { gr = st.rad[k]; g = k; }
+        if (g < 0) break;
+        const int a = st.far_idx[g];
+        // b = farthest (by centre distance) from a within g
+        for (int r = warp; r < nitems; r += nw) {
+            if (st.label[r] != g) continue;
+            const float dd = warp_dist(src + (int64_t)r * d, src + (int64_t)a * d, d);
+            if ((threadIdx.x & 31) == 0) st.dist[r] = dd;
+        }
+        __syncthreads();
+        float best = -1.f;
+        int bi = -1;
+        for (int r = threadIdx.x; r < nitems; r += blockDim.x)
+            if (st.label[r] == g && st.dist[r] > best) { best = st.dist[r]; bi = r; }
+        float v;
+        int b;
+        block_argmax(st, best, bi, v, b);
+        if (b < 0 || b == a || v <= 0.f) {
+            // nothing to split: mark the group unsplittable
+            if (threadIdx.x == 0) st.count[g] = 1;
+            __syncthreads();
+            continue;
+        }
+        const int ng = st.ngroups;
+        for (int r = warp; r < nitems; r += nw) {
+            if (st.label[r] != g) continue;
+            const float db = warp_dist(src + (int64_t)r * d, src + (int64_t)b * d, d);
+            if ((threadIdx.x & 31) == 0 && db < st.dist[r]) st.label[r] = ng;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) st.ngroups = ng + 1;
+        __syncthreads();
+        group_centroid(st, src, nitems, d, g, cen + (int64_t)g * d);
+        group_radius(st, src, irad, nitems, d, g, cen + (int64_t)g * d);
+        group_centroid(st, src, nitems, d, ng, cen + (int64_t)ng * d);
+        group_radius(st, src, irad, nitems, d, ng, cen + (int64_t)ng * d);
+        if (st.count[ng] == 0 || st.count[g] == 0) {
+            // degenerate split (all on one side): undo and stop splitting this group
+            for (int r = threadIdx.x; r < nitems; r += blockDim.x)
+                if (st.label[r] == ng) st.label[r] = g;
+            __syncthreads();
+            if (threadIdx.x == 0) st.ngroups = ng;
+            __syncthreads();
+            group_centroid(st, src, nitems, d, g, cen + (int64_t)g * d);
+            group_radius(st, src, irad, nitems, d, g, cen + (int64_t)g * d);
+            if (threadIdx.x == 0) st.count[g] = 1;
+            __syncthreads();
+        }
+    }
+}
+
+// One block per tile.  Output: centres [T][kBalls][d], radii [T][kBalls] (-1 = unused).
+__global__ void __launch_bounds__(256) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d, float grow,
+                                                    float* __restrict__ cen, float* __restrict__ rad)
+{
+    __shared__ BisectState st;
+    const int64_t t = blockIdx.x;
+    const int64_t r0 = t * kTile;
+    const int nitems = (int)min((int64_t)kTile, n - r0);
+    float* mycen = cen + t * kBalls * d;
+    bisect(st, Xs + r0 * d, nullptr, nitems, d, mycen);
+    if (threadIdx.x < kBalls)
+        rad[t * kBalls + threadIdx.x] = threadIdx.x < st.ngroups ? st.rad[threadIdx.x] * grow + 1e-30f : -1.f;
+}
+
+// One block per super-tile: balls over the (up to kSuper * kBalls) valid tile balls.
+__global__ void __launch_bounds__(256) k_super_balls(const float* __restrict__ tcen, const float* __restrict__ trad,
+                                                     int64_t T, int d, float grow, float* __restrict__ work,
+                                                     float* __restrict__ scen, float* __restrict__ srad)
+{
+    __shared__ BisectState st;
+    __shared__ float irad[kSuper * kBalls];
+    __shared__ int nvalid;
+    const int64_t s = blockIdx.x;
+    const int64_t t0 = s * kSuper, t1 = min(T, t0 + kSuper);
+    float* items = work + s * (int64_t)kSuper * kBalls * d;  // compacted valid ball centres
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int64_t t = t0; t < t1; ++t)
+            for (int k = 0; k < kBalls; ++k)
+                if (trad[t * kBalls + k] >= 0.f) irad[m++] = trad[t * kBalls + k];
+        nvalid = m;
+    }
+    __syncthreads();
+    // copy valid centres (same order as irad)
+    {
+        int m = 0;
+        for (int64_t t = t0; t < t1; ++t)
+            for (int k = 0; k < kBalls; ++k) {
+                if (trad[t * kBalls + k] < 0.f) continue;
+                for (int j = threadIdx.x; j < d; j += blockDim.x)
+                    items[(int64_t)m * d + j] = tcen[(t * kBalls + k) * (int64_t)d + j];
+                ++m;
+            }
+    }
+    __syncthreads();
+    bisect(st, items, irad, nvalid, d, scen + s * kBalls * d);
+    if (threadIdx.x < kBalls)
+        srad[s * kBalls + threadIdx.x] = threadIdx.x < st.ngroups ? st.rad[threadIdx.x] * grow + 1e-30f : -1.f;
+}
+
+// ------------------------------------------------------------------------------------------------
+// pruning
+
+// Level 1: all super-ball pairs as 128 x 32 distance blocks; a close ball pair marks
+// its super-tile pair (I <= J) in an S x S bitmap.
+__global__ void __launch_bounds__(256) k_super_close(const float* __restrict__ scen, const float* __restrict__ srad,
+                                                     int64_t NB, int d, float eps_p, float shrink,
+                                                     uint32_t* __restrict__ bitmap, int64_t S)
+{
+    __shared__ __align__(16) DistSmem sm;
+    const int64_t r0 = (int64_t)blockIdx.x * kDRows, c0 = (int64_t)blockIdx.y * kDCols;
+    if (c0 + kDCols <= r0 - kBalls) return;  // strictly below the diagonal of owners
+    float acc[4][4];
+    dist_block(sm, scen, nullptr, r0, NB, d, scen, c0, NB, acc);
+    const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int64_t row = r0 + ty * 4 + r;
+        if (row >= NB) continue;
+        const float rr = srad[row];
+        if (rr < 0.f) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int64_t col = c0 + tx * 4 + c;
+            if (col >= NB) continue;
+            const int64_t I = row / kBalls, J = col / kBalls;
+            if (I > J) continue;
+            const float rc = srad[col];
+            if (rc < 0.f) continue;
+            if (sqrtf(acc[r][c]) * shrink <= eps_p + rr + rc) {
+                const int64_t bit = I * S + J;
+                atomicOr(&bitmap[bit >> 5], 1u << (bit & 31));
+            }
+        }
+    }
+}
+
+__global__ void k_bitmap_pairs(const uint32_t* __restrict__ bitmap, int64_t S, int2* __restrict__ out,
+                               unsigned long long* __restrict__ count, unsigned long long cap)
+{
+    const int64_t words = (S * S + 31) / 32;
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t m = bitmap[w];
+        if (!m) continue;
+        const unsigned long long base = atomicAdd(count, (unsigned long long)__popc(m));
+        unsigned long long pos = base;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            const int64_t bit = w * 32 + b;
+            if (pos < cap) out[pos] = make_int2((int)(bit / S), (int)(bit % S));
+            ++pos;
+        }
+    }
+}
+
+// Level 2: one block per surviving super pair.  The two super-tiles' tile balls
+// (kSuper * kBalls each) are staged in shared memory 64 dimensions at a time; each
+// thread accumulates 4 of the 32 x 32 ball-pair distances; a tile pair survives
+// when any of its kBalls x kBalls ball pairs is close.
+constexpr int kNB = kSuper * kBalls;  // balls per super-tile
+constexpr int kDC = 64;               // dimensions per staged chunk
+
+__global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ supers,
+                                                    const unsigned long long* __restrict__ nsup_ptr,
+                                                    unsigned long long sup_cap, const float* __restrict__ tcen,
+                                                    const float* __restrict__ trad, int64_t T, int d, float eps_p,
+                                                    float shrink, int2* __restrict__ out,
+                                                    unsigned long long* __restrict__ count, unsigned long long cap)
+{
+    __shared__ float ca[kNB][kDC + 1], cb[kNB][kDC + 1];
+    __shared__ float ra[kNB], rb[kNB];
+    __shared__ int close_tile[kSuper][kSuper];
+    const unsigned long long nsup = min(*nsup_ptr, sup_cap);
+    for (unsigned long long w = blockIdx.x; w < nsup; w += gridDim.x) {
+        const int2 sp = supers[w];
+        const int64_t ta0 = (int64_t)sp.x * kSuper, tb0 = (int64_t)sp.y * kSuper;
+        for (int k = threadIdx.x; k < kNB; k += blockDim.x) {
+            const int64_t t1 = ta0 + k / kBalls, t2 = tb0 + k / kBalls;
+            ra[k] = t1 < T ? trad[t1 * kBalls + k % kBalls] : -1.f;
+            rb[k] = t2 < T ? trad[t2 * kBalls + k % kBalls] : -1.f;
+        }
+        for (int k = threadIdx.x; k < kSuper * kSuper; k += blockDim.x) close_tile[k / kSuper][k % kSuper] = 0;
+        // 2 x 2 ball pairs per thread: rows {ti, ti + 16}, columns {tj, tj + 16}
+        const int ti = threadIdx.x >> 4, tj = threadIdx.x & 15;
+        float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+        for (int k0 = 0; k0 < d; k0 += kDC) {
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < kNB * kDC; idx += blockDim.x) {
+                const int b = idx / kDC, k = k0 + idx % kDC;
+                const int64_t t1 = ta0 + b / kBalls, t2 = tb0 + b / kBalls;
+                ca[b][idx % kDC] = (t1 < T && k < d) ? tcen[(t1 * kBalls + b % kBalls) * (int64_t)d + k] : 0.f;
+                cb[b][idx % kDC] = (t2 < T && k < d) ? tcen[(t2 * kBalls + b % kBalls) * (int64_t)d + k] : 0.f;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int k = 0; k < kDC; ++k) {
+                const float a0 = ca[ti][k], a1 = ca[ti + 16][k], b0 = cb[tj][k], b1 = cb[tj + 16][k];
+                const float t00 = a0 - b0, t01 = a0 - b1, t10 = a1 - b0, t11 = a1 - b1;
+                acc[0][0] = fmaf(t00, t00, acc[0][0]);
+                acc[0][1] = fmaf(t01, t01, acc[0][1]);
+                acc[1][0] = fmaf(t10, t10, acc[1][0]);
+                acc[1][1] = fmaf(t11, t11, acc[1][1]);
+            }
+        }
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+                const int i = ti + 16 * x, j = tj + 16 * y;
+                if (ra[i] >= 0.f && rb[j] >= 0.f && sqrtf(acc[x][y]) * shrink <= eps_p + ra[i] + rb[j])
+                    close_tile[i / kBalls][j / kBalls] = 1;
+            }
+        __syncthreads();
+        if (threadIdx.x < kSuper * kSuper) {
+            const int qi = threadIdx.x / kSuper, qj = threadIdx.x % kSuper;
+            const int64_t i = ta0 + qi, j = tb0 + qj;
+            const bool keep = close_tile[qi][qj] && i < T && j < T && i <= j;
+            const unsigned ball = __ballot_sync(0xffffffffu, keep);
+            const int lane = threadIdx.x & 31;
+            unsigned long long base = 0;
+            if (lane == 0 && ball) base = atomicAdd(count, (unsigned long long)__popc(ball));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) {
+                const unsigned long long pos = base + __popc(ball & ((1u << lane) - 1u));
+                if (pos < cap) out[pos] = make_int2((int)i, (int)j);
+            }
+        }
+    }
+}
+
+// Schedule key of a tile pair for the tile kernels: (i mod G, i, j), so that after a
+// sort the pairs of CTA g (row tiles i = g, g + G, ...) are contiguous, each row's
+// column tiles ascend and CTAs sweep the same column tiles at about the same time.
+__global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, int G, uint64_t* __restrict__ keys)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        const int2 q = pairs[p];
+        keys[p] = ((uint64_t)(q.x % G) << 42) | ((uint64_t)q.x << 21) | (uint64_t)q.y;
+    }
+}
+
+__global__ void k_schedule_unpack(const uint64_t* __restrict__ keys, int64_t m, int2* __restrict__ pairs,
+                                  unsigned long long* __restrict__ starts)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[p];
+        pairs[p] = make_int2((int)((k >> 21) & 0x1fffff), (int)(k & 0x1fffff));
+        const uint64_t g = k >> 42;
+        if (p == 0 || (keys[p - 1] >> 42) != g) starts[g] = (unsigned long long)p;
+    }
+}
+
+__global__ void k_schedule_fix(unsigned long long* __restrict__ starts, int G)
+{
+    // CTAs without pairs get an empty range: starts[g] = starts[g + 1]
+    for (int g = G - 1; g >= 0; --g) starts[g] = min(starts[g], starts[g + 1]);
+}
+
+// ------------------------------------------------------------------------------------------------
+// host
+
+void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchild, const int32_t* child_off,
+                  int ncells, int32_t* rank)
+{
+    const size_t smem = sizeof(float) * kChainMax * (kChainMax - 1) / 2;
+    k_chain_leaves<<<ncells, 256, smem, c->stream>>>(lm_rows, d, nchild, child_off, rank);
+    RNNG_CUDA(cudaGetLastError());
+}
+
+void build_covers(rnng_ctx* c, Layout& L)
+{
+    cudaStream_t s = c->stream;
+    const float grow = 1.f + L.relerr;
+    c->tile_lo.reserve(sizeof(float) * (size_t)L.T * kBalls * L.d);   // tile ball centres
+    c->tile_hi.reserve(sizeof(float) * (size_t)L.T * kBalls);         // tile ball radii
+    c->super_lo.reserve(sizeof(float) * (size_t)L.S * kBalls * L.d);  // super ball centres
+    c->super_hi.reserve(sizeof(float) * (size_t)L.S * kBalls);        // super ball radii
+    c->pivots.reserve(sizeof(float) * (size_t)L.S * kSuper * kBalls * L.d);  // compaction workspace
+    k_tile_balls<<<(unsigned)L.T, 256, 0, s>>>(L.Xs, L.n, L.d, grow, c->tile_lo.as<float>(), c->tile_hi.as<float>());
+    k_super_balls<<<(unsigned)L.S, 256, 0, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d, grow,
+                                                c->pivots.as<float>(), c->super_lo.as<float>(),
+                                                c->super_hi.as<float>());
+    RNNG_CUDA(cudaGetLastError());
+}
+
+void prune_covers(rnng_ctx* c, Layout& L)
+{
+    cudaStream_t s = c->stream;
+    c->counters.reserve(sizeof(unsigned long long) * 8);
+    unsigned long long* cnt = c->counters.as<unsigned long long>();
+    const double u = 5.9604644775390625e-08;
+    const float eps_p = std::nextafter((float)((double)L.radius * (1.0 + (L.d + 8) * u) + 1e-30), INFINITY);
+    const float shrink = 1.f - L.relerr;
+    // level 1: bitmap of close super-tile pairs
+    const int64_t NB = L.S * kBalls;
+    const int64_t words = (L.S * L.S + 31) / 32;
+    c->aux6.reserve(sizeof(uint32_t) * (size_t)words);
+    uint32_t* bitmap = c->aux6.as<uint32_t>();
+    RNNG_CUDA(cudaMemsetAsync(bitmap, 0, sizeof(uint32_t) * (size_t)words, s));
+    dim3 g1((unsigned)ceil_div(NB, kDRows), (unsigned)ceil_div(NB, kDCols));
+    k_super_close<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), NB, L.d, eps_p, shrink, bitmap,
+                                     L.S);
+    unsigned long long sup_cap = std::max<unsigned long long>(4096, (unsigned long long)L.S * 64);
+    sup_cap = std::min<unsigned long long>(sup_cap, (unsigned long long)L.S * (L.S + 1) / 2);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        c->super_list.reserve(sizeof(int2) * sup_cap);
+        RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+        k_bitmap_pairs<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(words, 256), (int64_t)c->num_sms * 8)),
+                         256, 0, s>>>(bitmap, L.S, c->super_list.as<int2>(), cnt, sup_cap);
+        unsigned long long got = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        L.super_pairs = got;
+        if (got <= sup_cap) break;
+        sup_cap = got;
+    }
+    // level 2: tile pairs inside the surviving super pairs
+    const unsigned long long tile_cap =
+        std::max<unsigned long long>(1, L.super_pairs * (unsigned long long)(kSuper * kSuper));
+    c->pair_list.reserve(sizeof(int2) * tile_cap);
+    RNNG_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), s));
+    const unsigned grid = (unsigned)std::max<unsigned long long>(
+        1, std::min<unsigned long long>(L.super_pairs, (unsigned long long)c->num_sms * 16));
+    k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
+                                      c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(), cnt + 1,
+                                      tile_cap);
+    unsigned long long got = 0;
+    RNNG_CUDA(cudaMemcpyAsync(&got, cnt + 1, sizeof(got), cudaMemcpyDeviceToHost, s));
+    RNNG_CUDA(cudaStreamSynchronize(s));
+    L.tile_pairs = got;
+    L.pairs = c->pair_list.as<int2>();
+    L.d_tile_pairs = cnt + 1;
+}
+
+void schedule_pairs(rnng_ctx* c, Layout& L, int G)
+{
+    cudaStream_t s = c->stream;
+    const int64_t m = (int64_t)L.tile_pairs;
+    c->sched.reserve(sizeof(unsigned long long) * (G + 1));
+    unsigned long long* starts = c->sched.as<unsigned long long>();
+    L.sched = starts;
+    L.sched_G = G;
+    // every CTA's range starts empty (= m) until a boundary sets it
+    std::vector<unsigned long long> init(G + 1, (unsigned long long)m);
+    RNNG_CUDA(cudaMemcpyAsync(starts, init.data(), sizeof(unsigned long long) * (G + 1), cudaMemcpyHostToDevice, s));
+    if (m == 0) {
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    RNNG_REQUIRE(L.T < (1 << 21), RNNG_ERR_INVALID, "too many tiles for the tile-pair schedule");
+    c->aux6.reserve(sizeof(uint64_t) * 2 * (size_t)m);
+    uint64_t* k0 = c->aux6.as<uint64_t>();
+    uint64_t* k1 = k0 + m;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
+    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, G, k0);
+    size_t tmp = 0;
+    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, 64, s));
+    c->cub_tmp.reserve(tmp);
+    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, 64, s));
+    k_schedule_unpack<<<grid, 256, 0, s>>>(k1, m, L.pairs, starts);
+    k_schedule_fix<<<1, 1, 0, s>>>(starts, G);
+    RNNG_CUDA(cudaStreamSynchronize(s));  // init lifetime
+}
+
+}  // namespace rnng

@@ -79,7 +79,7 @@ struct rnng_ctx {
     // named scratch buffers
     rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
-        out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7;
+        out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;
     int64_t last_candidates = 0;
@@ -88,6 +88,8 @@ struct rnng_ctx {
     alignas(64) unsigned char tmap[128] = {};
     int bf16_dp = 0;
     void* bf16_rowinfo = nullptr;
+    void* bf16_ucol = nullptr;
+    void* bf16_tileinfo = nullptr;
     float bf16_eps_p = 0.f;
     int* fault_word = nullptr;  // device error word written by kernels with bounded waits
     cudaEvent_t ev[16] = {};

@@ -5,46 +5,33 @@
 // tree walk per query, the points are ordered by a two-level landmark partition
 // (the Voronoi idea of include/point.hpp:537-559 applied twice), cut into tiles of
 // 128 points, and every pair of tiles that the triangle inequality cannot rule out
-// is evaluated in full.  The pruning is exact: a tile pair is skipped only when a
-// pivot p gives |d(x,p) - d(y,p)| > radius for all x, y with a rounding slack that
-// covers the float error of both the pivot distances and the reference's own
-// sequential L2, so no pair with L2seq <= radius is ever skipped.
+// is evaluated in full.  The pruning is exact: a tile pair is skipped only when the
+// balls covering the two tiles are separated by more than the radius, with a
+// rounding slack that covers the float error of the ball geometry and of the
+// reference's own sequential L2, so no pair with L2seq <= radius is ever skipped.
 //
 // Stages (all on the context stream):
-//   1. level-1 landmarks (strided sample), nearest landmark per point  -> cell1
-//   2. sort by cell1; level-2 landmarks inside each cell1, nearest    -> leaf cell
-//   3. sort by (leaf, distance to its landmark); gather points in that order
-//   4. per tile and per pivot: [min, max] of the pivot distances
-//   5. prune super-tile pairs (8x8 tiles), then tile pairs
+//   1-3. recursive landmark partition: every cell larger than 2 tiles is split
+//      by up to kFan landmarks (strided picks from the cell), its points move to
+//      the nearest one, and the children are ordered along a nearest-neighbour
+//      chain; the points are sorted by (cell, distance to its landmark) after
+//      each level and finally gathered in that order.  Leaves hold about one
+//      tile, so a tile rarely mixes two clusters.
+//   4. cover every tile and super-tile (8 tiles) by a few balls (balls.cu)
+//   5. prune super-tile pairs, then tile pairs, by ball separation
 //   6. evaluate surviving tile pairs (FP32-direct here; BF16 Gram in gram_bf16.cu)
 //   7. map sorted indices back to ids, order each edge as u < v
 #include <cub/cub.cuh>
 
 #include "common.cuh"
 #include "eps_l2.cuh"
+#include "balls.cuh"
+#include "partition.cuh"
 
 namespace rnng {
 
 // ------------------------------------------------------------------------------------------------
 // helpers
-
-__device__ __forceinline__ float warp_sum(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Squared L2 (any summation order) of row x against row c, computed by one warp.
-__device__ __forceinline__ float warp_dist2(const float* __restrict__ x, const float* __restrict__ c, int d, int lane)
-{
-    float s = 0.f;
-    for (int k = lane; k < d; k += 32) {
-        float t = x[k] - c[k];
-        s = fmaf(t, t, s);
-    }
-    return warp_sum(s);
-}
 
 __global__ void k_gather_rows(const float* __restrict__ X, int64_t d, const int32_t* __restrict__ idx, int64_t m,
                               float* __restrict__ out)
@@ -62,39 +49,7 @@ __global__ void k_strided_index(int32_t* __restrict__ out, int64_t m, int64_t n)
     if (i < m) out[i] = (int32_t)((i * n) / m);
 }
 
-// Level 1: nearest of m1 landmarks for each point (warp per point).
-// key = (cell << 32) | bits(dist) so that a radix sort groups cells and orders
-// points by their distance to the cell landmark.
-__global__ void k_assign_level1(const float* __restrict__ X, int64_t n, int d, const float* __restrict__ L, int m1,
-                                uint64_t* __restrict__ keys, int32_t* __restrict__ vals)
-{
-    extern __shared__ float sL[];
-    const bool in_smem = (int64_t)m1 * d * 4 <= 48 * 1024;
-    if (in_smem)
-        for (int t = threadIdx.x; t < m1 * d; t += blockDim.x) sL[t] = L[t];
-    __syncthreads();
-    const float* LL = in_smem ? sL : L;
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = warp; i < n; i += nwarps) {
-        const float* x = X + i * d;
-        float best = INFINITY;
-        int bi = 0;
-        for (int c = 0; c < m1; ++c) {
-            float s = warp_dist2(x, LL + (int64_t)c * d, d, lane);
-            if (s < best) { best = s; bi = c; }
-        }
-        if (lane == 0) {
-            float dist = sqrtf(best);
-            keys[i] = ((uint64_t)bi << 32) | __float_as_uint(dist);
-            vals[i] = (int32_t)i;
-        }
-    }
-}
-
-// Per level-1 cell: start offset in the sorted order and size (cells are contiguous
-// after the sort).  One thread per sorted position marks cell boundaries.
+// Cell boundaries in the current order (cells are contiguous after each sort).
 __global__ void k_cell_bounds(const uint64_t* __restrict__ sorted_keys, int64_t n, int32_t* __restrict__ start,
                               int32_t* __restrict__ end)
 {
@@ -105,73 +60,30 @@ __global__ void k_cell_bounds(const uint64_t* __restrict__ sorted_keys, int64_t 
     if (i == n - 1 || (uint32_t)(sorted_keys[i + 1] >> 32) != c) end[c] = (int32_t)(i + 1);
 }
 
-// Level-2 landmark budget per level-1 cell (single block): m2[c] proportional to the
-// cell's size, at least 1 for a non-empty cell, at most kMaxSub; exclusive scan.
-__global__ void k_level2_plan(const int32_t* __restrict__ start, const int32_t* __restrict__ end, int m1, int64_t n,
-                              int64_t leaves_total, int32_t* __restrict__ m2, int32_t* __restrict__ m2_off)
+// Children per cell: cells above 2 * kLeafTarget points are split into
+// min(ceil(size / kLeafTarget), kFan) children, others keep one child.
+__global__ void k_split_plan(const int32_t* __restrict__ start, const int32_t* __restrict__ end, int64_t ncells,
+                             int32_t* __restrict__ nchild)
 {
-    __shared__ int32_t s[1024];
-    int c = threadIdx.x;
-    int v = 0;
-    if (c < m1) {
-        int sz = end[c] - start[c];
-        if (sz > 0) {
-            int64_t want = (leaves_total * sz + n - 1) / n;
-            v = (int)max((int64_t)1, min(want, (int64_t)kMaxSub));
-            v = min(v, sz);
-        }
-        m2[c] = v;
-    }
-    s[c] = v;
-    __syncthreads();
-    if (c == 0) {
-        int acc = 0;
-        for (int j = 0; j < m1; ++j) { int t = s[j]; s[j] = acc; acc += t; }
-        m2_off[m1] = acc;
-    }
-    __syncthreads();
-    if (c < m1) m2_off[c] = s[c];
+    int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int64_t sz = end[c] - start[c];
+    int64_t m = 1;
+    if (sz > 2 * kLeafTarget) m = min((sz + kLeafTarget - 1) / kLeafTarget, (int64_t)kFan);
+    nchild[c] = (int32_t)m;
 }
 
-// Level-2 landmark rows: sub-landmark k of cell c is the point at position
-// start[c] + floor(k * size / m2[c]) of the level-1 order.
-__global__ void k_level2_landmarks(const int32_t* __restrict__ start, const int32_t* __restrict__ end,
-                                   const int32_t* __restrict__ m2, const int32_t* __restrict__ m2_off, int m1,
-                                   const int32_t* __restrict__ order1, int32_t* __restrict__ sub_idx)
+// Landmark of child k of cell c: the point at position start + floor(k * size / m)
+// of the current order (its leading points are nearest the parent's landmark).
+__global__ void k_child_landmarks(const int32_t* __restrict__ start, const int32_t* __restrict__ end,
+                                  const int32_t* __restrict__ nchild, const int32_t* __restrict__ child_off,
+                                  int64_t ncells, const int32_t* __restrict__ order, int32_t* __restrict__ lm_idx)
 {
-    int c = blockIdx.x;
-    if (c >= m1) return;
-    int sz = end[c] - start[c];
-    for (int k = threadIdx.x; k < m2[c]; k += blockDim.x)
-        sub_idx[m2_off[c] + k] = order1[start[c] + (int)(((int64_t)k * sz) / m2[c])];
-}
-
-// Level 2: nearest sub-landmark inside the point's level-1 cell (warp per point,
-// points visited in level-1 order so a block's sub-landmarks stay in cache).
-__global__ void k_assign_level2(const float* __restrict__ X, int64_t n, int d, const uint64_t* __restrict__ keys1,
-                                const int32_t* __restrict__ order1, const float* __restrict__ SL,
-                                const int32_t* __restrict__ m2, const int32_t* __restrict__ m2_off,
-                                uint64_t* __restrict__ keys2, int32_t* __restrict__ vals2)
-{
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t p = warp; p < n; p += nwarps) {
-        int32_t i = order1[p];
-        int c = (int)(keys1[p] >> 32);
-        const float* x = X + (int64_t)i * d;
-        int base = m2_off[c], cnt = m2[c];
-        float best = INFINITY;
-        int bi = 0;
-        for (int k = 0; k < cnt; ++k) {
-            float s = warp_dist2(x, SL + (int64_t)(base + k) * d, d, lane);
-            if (s < best) { best = s; bi = k; }
-        }
-        if (lane == 0) {
-            keys2[p] = ((uint64_t)(base + bi) << 32) | __float_as_uint(sqrtf(best));
-            vals2[p] = i;
-        }
-    }
+    const int64_t c = blockIdx.x;
+    if (c >= ncells) return;
+    const int sz = end[c] - start[c], m = nchild[c];
+    for (int k = threadIdx.x; k < m; k += blockDim.x)
+        lm_idx[child_off[c] + k] = order[start[c] + (int)(((int64_t)k * sz) / m)];
 }
 
 // Sorted copy of the points, padded with zero rows to a multiple of the tile size.
@@ -182,133 +94,6 @@ __global__ void k_gather_sorted(const float* __restrict__ X, int64_t n, int64_t 
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t r = t / d, k = t - r * d;
         Xs[t] = (r < n) ? X[(int64_t)perm[r] * d + k] : 0.f;
-    }
-}
-
-// Per tile (128 sorted rows) and pivot: min and max of the pivot distance over the
-// tile's real rows.  Block = 4 warps = one tile; each warp covers 32 rows.
-// Output layout is [pivot][tile] so pruning threads read consecutive tiles.
-__global__ void k_tile_bounds(const float* __restrict__ Xs, int64_t n, int d, const float* __restrict__ Pv, int P,
-                              int64_t T, float* __restrict__ lo, float* __restrict__ hi)
-{
-    __shared__ float s_lo[4][kMaxPivots], s_hi[4][kMaxPivots];
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t t = blockIdx.x;
-    for (int p = lane; p < P; p += 32) { s_lo[warp][p] = INFINITY; s_hi[warp][p] = -INFINITY; }
-    __syncwarp();
-    for (int r = 0; r < 32; ++r) {
-        int64_t row = t * kTile + warp * 32 + r;
-        if (row >= n) break;
-        const float* x = Xs + row * d;
-        for (int p = 0; p < P; ++p) {
-            float s = sqrtf(warp_dist2(x, Pv + (int64_t)p * d, d, lane));
-            if (lane == 0) {
-                s_lo[warp][p] = fminf(s_lo[warp][p], s);
-                s_hi[warp][p] = fmaxf(s_hi[warp][p], s);
-            }
-        }
-    }
-    __syncthreads();
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        float a = fminf(fminf(s_lo[0][p], s_lo[1][p]), fminf(s_lo[2][p], s_lo[3][p]));
-        float b = fmaxf(fmaxf(s_hi[0][p], s_hi[1][p]), fmaxf(s_hi[2][p], s_hi[3][p]));
-        lo[(int64_t)p * T + t] = a;
-        hi[(int64_t)p * T + t] = b;
-    }
-}
-
-// Super-tile bounds: union of kSuper consecutive tiles' intervals.
-__global__ void k_super_bounds(const float* __restrict__ lo, const float* __restrict__ hi, int P, int64_t T, int64_t S,
-                               float* __restrict__ slo, float* __restrict__ shi)
-{
-    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)P * S) return;
-    int64_t p = t / S, s = t - p * S;
-    float a = INFINITY, b = -INFINITY;
-    for (int64_t k = s * kSuper; k < min(T, (s + 1) * kSuper); ++k) {
-        a = fminf(a, lo[p * T + k]);
-        b = fmaxf(b, hi[p * T + k]);
-    }
-    slo[p * S + s] = a;
-    shi[p * S + s] = b;
-}
-
-// True when some pivot separates the two intervals by more than the radius plus
-// the rounding slack.  relerr bounds the relative error of every computed distance
-// (pivot distances here and the reference's sequential L2), so skipping is exact.
-__device__ __forceinline__ bool separated(float loA, float hiA, float loB, float hiB, float radius, float relerr)
-{
-    float g1 = loB - hiA, g2 = loA - hiB;
-    float thr1 = radius + relerr * (radius + loB + hiA) + 1e-30f;
-    float thr2 = radius + relerr * (radius + loA + hiB) + 1e-30f;
-    return (g1 > thr1) || (g2 > thr2);
-}
-
-// Level 1 of the pruning: super-tile pairs (I <= J).  blockIdx.y = I.
-__global__ void k_prune_super(const float* __restrict__ slo, const float* __restrict__ shi, int P, int64_t S,
-                              float radius, float relerr, int2* __restrict__ out, unsigned long long* __restrict__ count,
-                              unsigned long long cap)
-{
-    int64_t I = blockIdx.y;
-    int64_t J = I + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    bool keep = false;
-    if (J < S) {
-        keep = true;
-        for (int p = 0; p < P; ++p) {
-            if (separated(slo[p * S + I], shi[p * S + I], slo[p * S + J], shi[p * S + J], radius, relerr)) {
-                keep = false;
-                break;
-            }
-        }
-    }
-    unsigned mask = __ballot_sync(0xffffffffu, keep);
-    if (!mask) return;
-    int lane = threadIdx.x & 31;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) {
-        unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
-        if (pos < cap) out[pos] = make_int2((int)I, (int)J);
-    }
-}
-
-// Level 2: the tile pairs (i <= j) inside each surviving super pair.  One warp per
-// super pair, kSuper*kSuper = 64 tile pairs, two per lane.
-__global__ void k_prune_tiles(const int2* __restrict__ supers, const unsigned long long* __restrict__ nsup_ptr,
-                              unsigned long long sup_cap, const float* __restrict__ lo, const float* __restrict__ hi,
-                              int P, int64_t T, float radius, float relerr, int2* __restrict__ out,
-                              unsigned long long* __restrict__ count, unsigned long long cap)
-{
-    unsigned long long nsup = min(*nsup_ptr, sup_cap);
-    int lane = threadIdx.x & 31;
-    int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t w = warp; w < (int64_t)nsup; w += nwarps) {
-        int2 sp = supers[w];
-        for (int half = 0; half < 2; ++half) {
-            int q = lane + 32 * half;
-            int64_t i = (int64_t)sp.x * kSuper + (q / kSuper);
-            int64_t j = (int64_t)sp.y * kSuper + (q % kSuper);
-            bool keep = (i < T) && (j < T) && (i <= j);
-            if (keep) {
-                for (int p = 0; p < P; ++p) {
-                    if (separated(lo[p * T + i], hi[p * T + i], lo[p * T + j], hi[p * T + j], radius, relerr)) {
-                        keep = false;
-                        break;
-                    }
-                }
-            }
-            unsigned mask = __ballot_sync(0xffffffffu, keep);
-            if (!mask) continue;
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(mask));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep) {
-                unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
-                if (pos < cap) out[pos] = make_int2((int)i, (int)j);
-            }
-        }
     }
 }
 
@@ -435,8 +220,26 @@ __global__ void k_finalize_edges(const uint32_t* __restrict__ si, const uint32_t
     }
 }
 
+__global__ void k_iota_keys(int32_t* __restrict__ order, uint64_t* __restrict__ keys, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        order[i] = (int32_t)i;
+        keys[i] = 0ull;
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // host side
+
+void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t count)
+{
+    // count includes the trailing total: in[count-1] is read as 0 by scanning count-1 items
+    size_t tmp = 0;
+    RNNG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int)count, c->stream));
+    c->cub_tmp.reserve(tmp);
+    RNNG_CUDA(cudaMemsetAsync((void*)(in + count - 1), 0, sizeof(int32_t), c->stream));
+    RNNG_CUDA(cub::DeviceScan::ExclusiveSum(c->cub_tmp.ptr, tmp, in, out, (int)count, c->stream));
+}
 
 static int grid_for(rnng_ctx* c, int64_t work, int per_block, int waves = 8)
 {
@@ -475,128 +278,57 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     L.S = ceil_div(L.T, kSuper);
     cudaStream_t s = c->stream;
 
-    // ---- level 1
-    int64_t leaves = std::max<int64_t>(1, std::min<int64_t>(n / kLeafTarget, kMaxLeaves));
-    int m1 = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::ceil(std::sqrt((double)leaves)), kMaxSub));
-    if (m1 > n) m1 = (int)n;
-    L.m1 = m1;
-    c->aux0.reserve(sizeof(int32_t) * (m1 + 1));
-    c->aux1.reserve(sizeof(float) * (size_t)m1 * d);
-    int32_t* l1_idx = c->aux0.as<int32_t>();
-    float* l1_rows = c->aux1.as<float>();
-    k_strided_index<<<ceil_div(m1, 256), 256, 0, s>>>(l1_idx, m1, n);
-    k_gather_rows<<<grid_for(c, (int64_t)m1 * d, 256), 256, 0, s>>>(dX, d, l1_idx, m1, l1_rows);
+    // current order and sorted keys (cell << 32 | distance bits); start: one cell
     c->keys.reserve(sizeof(uint64_t) * n);
     c->keys_alt.reserve(sizeof(uint64_t) * n);
     c->perm.reserve(sizeof(int32_t) * L.n_pad);
     c->perm_alt.reserve(sizeof(int32_t) * n);
-    uint64_t* k1 = c->keys.as<uint64_t>();
-    uint64_t* k1s = c->keys_alt.as<uint64_t>();
-    int32_t* v1 = c->perm_alt.as<int32_t>();
-    int32_t* order1 = c->perm.as<int32_t>();
-    size_t smem1 = ((int64_t)m1 * d * 4 <= 48 * 1024) ? (size_t)m1 * d * 4 : 0;
-    k_assign_level1<<<grid_for(c, n * 32, 256), 256, smem1, s>>>(dX, n, d, l1_rows, m1, k1, v1);
-    sort_pairs_u64(c, k1, k1s, v1, order1, n, 32 + bits_for(m1));
-
-    // ---- level 2
-    c->aux2.reserve(sizeof(int32_t) * (4 * (size_t)m1 + 4));
+    uint64_t* skeys = c->keys_alt.as<uint64_t>();   // sorted keys of the current order
+    uint64_t* nkeys = c->keys.as<uint64_t>();       // keys of the next level, in current order
+    int32_t* order = c->perm.as<int32_t>();          // current order: position -> input row
+    int32_t* nvals = c->perm_alt.as<int32_t>();
+    k_iota_keys<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), (int64_t)c->num_sms * 8), 256, 0, s>>>(order, skeys, n);
+    int64_t ncells = 1;
+    // per-cell scratch (cells never outnumber points)
+    const int64_t cap = n + 2;
+    c->aux2.reserve(sizeof(int32_t) * (size_t)(4 * cap + 4));
     int32_t* cstart = c->aux2.as<int32_t>();
-    int32_t* cend = cstart + m1;
-    int32_t* m2 = cend + m1;
-    int32_t* m2_off = m2 + m1;
-    RNNG_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int32_t) * 2 * m1, s));
-    k_cell_bounds<<<ceil_div(n, 256), 256, 0, s>>>(k1s, n, cstart, cend);
-    k_level2_plan<<<1, 1024, 0, s>>>(cstart, cend, m1, n, leaves, m2, m2_off);
-    int64_t max_sub = (int64_t)m1 * kMaxSub;
-    c->aux3.reserve(sizeof(int32_t) * max_sub);
-    c->aux4.reserve(sizeof(float) * (size_t)max_sub * d);
-    int32_t* sub_idx = c->aux3.as<int32_t>();
-    float* sub_rows = c->aux4.as<float>();
-    k_level2_landmarks<<<m1, 128, 0, s>>>(cstart, cend, m2, m2_off, m1, order1, sub_idx);
-    int32_t total_sub = 0;
-    RNNG_CUDA(cudaMemcpyAsync(&total_sub, m2_off + m1, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    RNNG_CUDA(cudaStreamSynchronize(s));
-    L.num_cells = total_sub;
-    k_gather_rows<<<grid_for(c, (int64_t)total_sub * d, 256), 256, 0, s>>>(dX, d, sub_idx, total_sub, sub_rows);
-    uint64_t* k2 = k1;  // reuse
-    int32_t* v2 = v1;
-    k_assign_level2<<<grid_for(c, n * 32, 256), 256, 0, s>>>(dX, n, d, k1s, order1, sub_rows, m2, m2_off, k2, v2);
-    int32_t* perm = order1;  // final order overwrites the level-1 order
-    sort_pairs_u64(c, k2, k1s, v2, perm, n, 32 + bits_for(total_sub));
-    L.perm = perm;
+    int32_t* cend = cstart + cap;
+    int32_t* nchild = cend + cap;
+    int32_t* child_off = nchild + cap;
+    int levels = 0;
+    for (; levels < kMaxLevels; ++levels) {
+        k_cell_bounds<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(skeys, n, cstart, cend);
+        k_split_plan<<<(unsigned)ceil_div(ncells, 256), 256, 0, s>>>(cstart, cend, ncells, nchild);
+        exclusive_scan_i32(c, nchild, child_off, ncells + 1);
+        int32_t total = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&total, child_off + ncells, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        if (total == ncells) break;  // every cell is a leaf
+        c->aux3.reserve(sizeof(int32_t) * (size_t)total);
+        c->aux4.reserve(sizeof(float) * (size_t)total * d);
+        c->aux5.reserve(sizeof(int32_t) * (size_t)total);
+        int32_t* lm_idx = c->aux3.as<int32_t>();
+        float* lm_rows = c->aux4.as<float>();
+        k_child_landmarks<<<(unsigned)ncells, 64, 0, s>>>(cstart, cend, nchild, child_off, ncells, order, lm_idx);
+        k_gather_rows<<<grid_for(c, (int64_t)total * d, 256), 256, 0, s>>>(dX, d, lm_idx, total, lm_rows);
+        // children ordered along a greedy nearest-neighbour chain of their landmarks
+        chain_leaves(c, lm_rows, d, nchild, child_off, (int)ncells, c->aux5.as<int32_t>());
+        launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, c->aux5.as<int32_t>(), nkeys, nvals);
+        sort_pairs_u64(c, nkeys, skeys, nvals, order, n, 32 + bits_for(total));
+        ncells = total;
+    }
+    L.num_cells = ncells;
+    L.m1 = levels;
+    L.perm = order;
 
     // ---- sorted points
     c->x_sorted.reserve(sizeof(float) * (size_t)L.n_pad * d);
     L.Xs = c->x_sorted.as<float>();
-    k_gather_sorted<<<grid_for(c, L.n_pad * d, 256), 256, 0, s>>>(dX, n, L.n_pad, d, perm, L.Xs);
-
-    // ---- pivots: a strided subset of the leaf landmarks
-    int P = (int)std::min<int64_t>(kMaxPivots, total_sub);
-    L.P = P;
-    c->pivots.reserve(sizeof(float) * (size_t)P * d);
-    c->aux5.reserve(sizeof(int32_t) * P);
-    {
-        // pivot k = leaf landmark floor(k * total_sub / P): gather through sub_idx
-        std::vector<int32_t> hidx(P);
-        for (int k = 0; k < P; ++k) hidx[k] = (int32_t)(((int64_t)k * total_sub) / P);
-        RNNG_CUDA(cudaMemcpyAsync(c->aux5.ptr, hidx.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, s));
-        k_gather_rows<<<grid_for(c, (int64_t)P * d, 256), 256, 0, s>>>(sub_rows, d, c->aux5.as<int32_t>(), P,
-                                                                       c->pivots.as<float>());
-        RNNG_CUDA(cudaStreamSynchronize(s));  // hidx lifetime
-    }
+    k_gather_sorted<<<grid_for(c, L.n_pad * d, 256), 256, 0, s>>>(dX, n, L.n_pad, d, order, L.Xs);
     L.relerr = (float)((d + 16) * 1.1920928955078125e-07);  // (d+16) * 2^-23
     L.radius = radius;
     return L;
-}
-
-void compute_bounds(rnng_ctx* c, Layout& L)
-{
-    cudaStream_t s = c->stream;
-    c->tile_lo.reserve(sizeof(float) * (size_t)L.P * L.T);
-    c->tile_hi.reserve(sizeof(float) * (size_t)L.P * L.T);
-    c->super_lo.reserve(sizeof(float) * (size_t)L.P * L.S);
-    c->super_hi.reserve(sizeof(float) * (size_t)L.P * L.S);
-    k_tile_bounds<<<(unsigned)L.T, 128, 0, s>>>(L.Xs, L.n, L.d, c->pivots.as<float>(), L.P, L.T,
-                                                 c->tile_lo.as<float>(), c->tile_hi.as<float>());
-    k_super_bounds<<<ceil_div((int64_t)L.P * L.S, 256), 256, 0, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(),
-                                                                     L.P, L.T, L.S, c->super_lo.as<float>(),
-                                                                     c->super_hi.as<float>());
-}
-
-void prune(rnng_ctx* c, Layout& L)
-{
-    cudaStream_t s = c->stream;
-    c->counters.reserve(sizeof(unsigned long long) * 8);
-    unsigned long long* cnt = c->counters.as<unsigned long long>();
-    RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 8, s));
-    // super pairs: worst case S(S+1)/2, bounded by memory; grown on overflow
-    unsigned long long sup_cap = std::max<unsigned long long>(1024, (unsigned long long)L.S * 64);
-    sup_cap = std::min<unsigned long long>(sup_cap, (unsigned long long)L.S * (L.S + 1) / 2);
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        c->super_list.reserve(sizeof(int2) * sup_cap);
-        RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
-        dim3 g1((unsigned)ceil_div(L.S, 256), (unsigned)L.S);
-        k_prune_super<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), L.P, L.S, L.radius,
-                                         L.relerr, c->super_list.as<int2>(), cnt, sup_cap);
-        unsigned long long got = 0;
-        RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
-        RNNG_CUDA(cudaStreamSynchronize(s));
-        L.super_pairs = got;
-        if (got <= sup_cap) break;
-        sup_cap = got;
-    }
-    unsigned long long tile_cap = std::max<unsigned long long>(1, L.super_pairs * (unsigned long long)(kSuper * kSuper));
-    c->pair_list.reserve(sizeof(int2) * tile_cap);
-    RNNG_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), s));
-    k_prune_tiles<<<grid_for(c, (int64_t)L.super_pairs * 32, 256), 256, 0, s>>>(
-        c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.P, L.T,
-        L.radius, L.relerr, c->pair_list.as<int2>(), cnt + 1, tile_cap);
-    unsigned long long got = 0;
-    RNNG_CUDA(cudaMemcpyAsync(&got, cnt + 1, sizeof(got), cudaMemcpyDeviceToHost, s));
-    RNNG_CUDA(cudaStreamSynchronize(s));
-    L.tile_pairs = got;
-    L.pairs = c->pair_list.as<int2>();
-    L.d_tile_pairs = cnt + 1;
 }
 
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E)

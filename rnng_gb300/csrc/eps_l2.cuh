@@ -9,15 +9,15 @@ namespace rnng {
 
 constexpr int kTile = 128;          // points per tile (one tcgen05 M=128 / N=128 operand)
 constexpr int kSuper = 8;           // tiles per super-tile in the first pruning level
-constexpr int kMaxPivots = 64;      // pivots used for interval pruning
-constexpr int kMaxSub = 64;         // level-2 landmarks per level-1 cell (and level-1 count)
-constexpr int64_t kLeafTarget = 512;  // points per leaf cell
-constexpr int64_t kMaxLeaves = 4096;
+constexpr int kBalls = 4;           // balls covering one tile (and one super-tile)
+constexpr int kFan = 64;            // children per split of the landmark partition
+constexpr int64_t kLeafTarget = 128;  // points per leaf cell
+constexpr int kMaxLevels = 8;       // depth limit of the partition
 
 // Device layout of one epsilon-graph problem after the partition.
 struct Layout {
     int64_t n = 0, n_pad = 0, T = 0, S = 0;
-    int d = 0, m1 = 0, P = 0;
+    int d = 0, m1 = 0;
     int64_t num_cells = 0;
     float radius = 0.f, relerr = 0.f;
     float* Xs = nullptr;          // n_pad x d, sorted by leaf cell, zero padded
@@ -25,6 +25,8 @@ struct Layout {
     unsigned long long super_pairs = 0, tile_pairs = 0;
     int2* pairs = nullptr;        // surviving tile pairs (i <= j)
     unsigned long long* d_tile_pairs = nullptr;  // device copy of tile_pairs
+    unsigned long long* sched = nullptr;          // per-CTA ranges of the pair list (G + 1 entries)
+    int sched_G = 0;
 };
 
 // Edge buffer in sorted-index space.
@@ -37,13 +39,13 @@ struct EdgeOut {
 };
 
 Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius);
-void compute_bounds(rnng_ctx* c, Layout& L);
-void prune(rnng_ctx* c, Layout& L);
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E);
 void finalize_edges(rnng_ctx* c, const Layout& L, const int64_t* d_ids, const EdgeOut& E, int64_t m, int64_t* u,
                     int64_t* v, float* w);
 void sort_pairs_u64(rnng_ctx* c, uint64_t* keys_in, uint64_t* keys_out, int32_t* vals_in, int32_t* vals_out,
                     int64_t n, int end_bit);
+// out[0..count-1] = exclusive prefix sum of in[0..count-2] (in[count-1] is zeroed first).
+void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t count);
 
 // BF16 tensor-core Gram tiles with FP32 recheck (gram_bf16.cu).
 void prepare_bf16(rnng_ctx* c, Layout& L);

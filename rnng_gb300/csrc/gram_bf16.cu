@@ -17,12 +17,14 @@
 // separate kernel: the edge set and every weight are exactly the reference's.
 //
 // Kernel roles (one CTA per SM, persistent over the tile-pair list):
-//   warp 0      TMA producer: K-chunks of 64 BF16 (one 128 B swizzle span) of the
-//               A tile (rows of I) and B tile (rows of J) into a 4-stage ring
-//   warp 1      MMA issuer: 4 x (M=128, N=128, K=16) per chunk into one of two
-//               TMEM accumulators (2 x 128 columns)
-//   warps 2-5   epilogue: tcgen05.ld of the accumulator rows (one TMEM lane per
-//               point of I), candidate test, warp-aggregated append
+//   warp 0      TMA producer: the A tile (rows of I, all K-chunks of 64 BF16 = one
+//               128 B swizzle span each) into a resident buffer when I changes, and
+//               the B tile (rows of J, all K-chunks) into a ring of item slots
+//   warp 1      MMA issuer: 4 x (M=128, N=128, K=16) per chunk into one of four
+//               TMEM accumulators (4 x 128 columns), one commit per item
+//   warps 2-9   epilogue: 2 warps per TMEM sub-partition, each reads a 32 x 64
+//               slice of the accumulator (one lane per point of I), tests it and
+//               appends candidates with one atomic per warp
 // Every mbarrier wait is bounded (about one second of wall time); on timeout the
 // CTA records a fault code in the context's fault word, stops issuing work, waits
 // (bounded) for its own copies and MMAs in flight and frees its tensor memory.
@@ -37,22 +39,28 @@
 
 namespace rnng {
 
-constexpr int kNS = 4;                              // shared-memory ring stages
-constexpr int kChunkK = 64;                         // BF16 elements per K-chunk
-constexpr int kChunkBytes = kTile * kChunkK * 2;    // 16 KB per operand per chunk
-constexpr int kStageBytes = 2 * kChunkBytes;        // A + B
+constexpr int kChunkK = 64;                         // BF16 elements per K-chunk (one 128 B swizzle span)
+constexpr int kChunkBytes = kTile * kChunkK * 2;    // 16 KB per operand tile per chunk
+constexpr int kMaxDp = 256;                         // padded dimension limit of the BF16 path
+constexpr int kRingBytes = 8 * kChunkBytes;         // B-operand ring: item slots of kchunks chunks
+constexpr int kMaxSlots = 8;
 constexpr int kAccCols = 128;                       // fp32 accumulator columns (N)
-constexpr int kTmemCols = 2 * kAccCols;
-constexpr int kEpiWarps = 4;
-constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 192
+constexpr int kAccBufs = 4;                         // accumulators in tensor memory
+constexpr int kTmemCols = kAccBufs * kAccCols;      // all 512 columns
+constexpr int kEpiGroups = 2;                       // epilogue groups, taking alternate items
+constexpr int kGroupWarps = 8;                      // per group: 2 per TMEM sub-partition
+constexpr int kEpiWarps = kEpiGroups * kGroupWarps;
+constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 576
+constexpr int kEpiCols = kAccCols / (kGroupWarps / 4);  // accumulator columns per epilogue warp (64)
 constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
 
 struct GramSmem {
     // offsets inside the dynamic shared block (which is 1024-aligned)
-    static constexpr int stages = 0;
-    static constexpr int colinfo = kNS * kStageBytes;                   // kEpiWarps x 128 float4
-    static constexpr int bars = colinfo + kEpiWarps * kTile * 16;       // mbarriers
-    static constexpr int nbars = 2 * kNS + 2 + 2 + 1;                   // full, empty, tfull, tempty, drain
+    static constexpr int a_tile = 0;                                    // resident A tile, kMaxDp/64 chunks
+    static constexpr int b_ring = (kMaxDp / kChunkK) * kChunkBytes;     // B item slots
+    static constexpr int colinfo = b_ring + kRingBytes;                 // kEpiWarps x kEpiCols floats (u_j)
+    static constexpr int bars = colinfo + kEpiWarps * kEpiCols * 4;     // mbarriers
+    static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1;  // a_full/empty, b_full/empty, tfull/tempty, drain
     static constexpr int misc = bars + nbars * 8;                       // tmem slot, abort flag
     static constexpr int total = misc + 16;
 };
@@ -118,6 +126,14 @@ __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile 
             }
         }
     }
+}
+
+// Inline fast path (one try_wait), then the bounded wait.
+__device__ __forceinline__ bool mbar_wait_fast(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* fault,
+                                               int where)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    return mbar_wait(bar, parity, abort_flag, fault, where);
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
@@ -199,24 +215,67 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kAccCols >> 3) << 17) |
                             ((uint32_t)(kTile >> 4) << 24);
 
+// Four-deep register prefetch of the tile-pair list, so that the dependent global
+// load of the next item's indices is issued several items ahead of its use.
+struct PairPrefetch {
+    int2 q0, q1, q2, q3;
+    const int2* __restrict__ p;
+    unsigned long long end;
+    unsigned stride;
+    __device__ __forceinline__ int2 ld(unsigned long long w) const { return w < end ? p[w] : make_int2(-1, -1); }
+    __device__ __forceinline__ void init(const int2* __restrict__ pairs, unsigned long long w, unsigned long long e,
+                                         unsigned step = 1)
+    {
+        p = pairs;
+        end = e;
+        stride = step;
+        q0 = ld(w);
+        q1 = ld(w + step);
+        q2 = ld(w + 2 * step);
+        q3 = ld(w + 3 * step);
+    }
+    // returns item w (the next item of this sequence) and prefetches item w + 4 * stride
+    __device__ __forceinline__ int2 next(unsigned long long w)
+    {
+        const int2 r = q0;
+        q0 = q1;
+        q1 = q2;
+        q2 = q3;
+        q3 = ld(w + 4ull * stride);
+        return r;
+    }
+};
+
 // ------------------------------------------------------------------------------------------------
 // the Gram kernel
+//
+// CTA g takes its range of the scheduled tile-pair list: row tiles i = g, g + G, ...
+// in order, each with its column tiles ascending.  The A tile (rows of i, all
+// K-chunks) stays resident in shared memory for the whole row, only B tiles stream
+// through the ring, and all CTAs sweep similar column tiles at the same time so
+// that B tiles are shared through L2.
 
 __global__ void __launch_bounds__(kGramThreads, 1)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int2* __restrict__ pairs,
                 const unsigned long long* __restrict__ npairs_ptr, unsigned long long pair_cap, int kchunks,
-                const float4* __restrict__ rowinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
-                unsigned long long* __restrict__ cand_count, unsigned long long cand_cap, int* __restrict__ fault)
+                const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
+                const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
+                unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
+                const unsigned long long* __restrict__ sched, int* __restrict__ fault)
 {
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
-    // align the dynamic block to 1024 bytes (swizzle atoms)
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(sm + GramSmem::bars);
-    uint64_t* full = bars;
-    uint64_t* empty = bars + kNS;
-    uint64_t* tfull = bars + 2 * kNS;
-    uint64_t* tempty = bars + 2 * kNS + 2;
-    uint64_t* drain = bars + 2 * kNS + 4;
+    uint64_t* a_full = bars;
+    uint64_t* a_empty = bars + 1;
+    uint64_t* b_full = bars + 2;
+    uint64_t* b_empty = bars + 2 + kMaxSlots;
+    uint64_t* tfull = bars + 2 + 2 * kMaxSlots;
+    uint64_t* tempty = tfull + kAccBufs;
+    uint64_t* drain = tempty + kAccBufs;
+    // ring slots: one item (all K-chunks of its B tile) per slot
+    const int nslots = min(kMaxSlots, kRingBytes / (kchunks * kChunkBytes));
+    const uint32_t slot_bytes = (uint32_t)(kchunks * kChunkBytes);
     uint32_t* tmem_slot = (uint32_t*)(sm + GramSmem::misc);
     volatile int* abort_flag = (volatile int*)(sm + GramSmem::misc + 4);
 
@@ -226,13 +285,15 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         tmem_relinquish();
     }
     if (threadIdx.x == 32) {
-        for (int s = 0; s < kNS; ++s) {
-            mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+        mbar_init(a_full, 1);
+        mbar_init(a_empty, 1);
+        for (int s = 0; s < kMaxSlots; ++s) {
+            mbar_init(&b_full[s], 1);
+            mbar_init(&b_empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kAccBufs; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], kEpiWarps);
+            mbar_init(&tempty[b], kGroupWarps);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -244,36 +305,53 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     const unsigned long long npairs = min(*npairs_ptr, pair_cap);
+    const unsigned long long wbeg = min(npairs, sched[blockIdx.x]);
+    const unsigned long long wend = min(npairs, sched[blockIdx.x + 1]);
 
     if (warp == 0) {
         if (lane == 0) {
             // ---------------- TMA producer
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
-            uint32_t it = 0;
-            uint32_t last_phase[kNS];
-            bool issued[kNS];
-            for (int s = 0; s < kNS; ++s) { issued[s] = false; last_phase[s] = 0; }
+            uint32_t aloads = 0;
+            int cur_i = -1;
+            uint32_t last_phase[kMaxSlots];
+            bool issued[kMaxSlots];
+            for (int q = 0; q < kMaxSlots; ++q) { issued[q] = false; last_phase[q] = 0; }
             bool ok = true;
-            for (unsigned long long w = blockIdx.x; ok && w < npairs; w += gridDim.x) {
-                const int2 tp = pairs[w];
-                for (int kc = 0; kc < kchunks; ++kc, ++it) {
-                    const int s = it % kNS;
-                    const uint32_t ph = (it / kNS) & 1u;
-                    if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag, fault, 1)) { ok = false; break; }
-                    uint8_t* st = sm + GramSmem::stages + s * kStageBytes;
-                    mbar_expect_tx(&full[s], kStageBytes);
-                    tma_load_2d(st, &tmap, &full[s], kc * kChunkK, tp.x * kTile);
-                    tma_load_2d(st + kChunkBytes, &tmap, &full[s], kc * kChunkK, tp.y * kTile);
-                    issued[s] = true;
-                    last_phase[s] = ph;
+            PairPrefetch pf;
+            pf.init(pairs, wbeg, wend);
+            uint32_t it = 0;
+            for (unsigned long long w = wbeg; ok && w < wend; ++w, ++it) {
+                const int2 tp = pf.next(w);
+                if (tp.x != cur_i) {
+                    if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
+                    mbar_expect_tx(a_full, slot_bytes);
+                    for (int kc = 0; kc < kchunks; ++kc)
+                        tma_load_2d(sm + GramSmem::a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK,
+                                    tp.x * kTile);
+                    ++aloads;
+                    cur_i = tp.x;
                 }
+                const int q = (int)(it % (uint32_t)nslots);
+                const uint32_t ph = (it / (uint32_t)nslots) & 1u;
+                if (!mbar_wait_fast(&b_empty[q], ph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
+                mbar_expect_tx(&b_full[q], slot_bytes);
+                uint8_t* slot = sm + GramSmem::b_ring + q * slot_bytes;
+                for (int kc = 0; kc < kchunks; ++kc)
+                    tma_load_2d(slot + kc * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, tp.y * kTile);
+                issued[q] = true;
+                last_phase[q] = ph;
             }
             if (!ok) {
-                // drain: every stage's most recent copy must land before the CTA exits
-                for (int s = 0; s < kNS; ++s) {
-                    if (!issued[s]) continue;
-                    uint64_t t0 = globaltimer();
-                    while (!mbar_try_wait(&full[s], last_phase[s]) && globaltimer() - t0 < kWaitNs) {
+                // drain: the copies in flight must land before the CTA exits
+                uint64_t t0 = globaltimer();
+                if (aloads > 0)
+                    while (!mbar_try_wait(a_full, (aloads - 1) & 1u) && globaltimer() - t0 < kWaitNs) {
+                    }
+                for (int q = 0; q < kMaxSlots; ++q) {
+                    if (!issued[q]) continue;
+                    t0 = globaltimer();
+                    while (!mbar_try_wait(&b_full[q], last_phase[q]) && globaltimer() - t0 < kWaitNs) {
                     }
                 }
             }
@@ -281,30 +359,42 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             // ---------------- MMA issuer
-            uint32_t it = 0, local = 0;
+            uint32_t local = 0, aidx = 0;
+            int cur_i = -1;
             bool ok = true, any = false;
-            for (unsigned long long w = blockIdx.x; ok && w < npairs; w += gridDim.x, ++local) {
-                const int b = local & 1;
-                const uint32_t tph = (local >> 1) & 1u;
-                if (!mbar_wait(&tempty[b], tph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
+            PairPrefetch pf;
+            pf.init(pairs, wbeg, wend);
+            for (unsigned long long w = wbeg; ok && w < wend; ++w, ++local) {
+                const int2 tp = pf.next(w);
+                if (tp.x != cur_i) {
+                    if (!mbar_wait_fast(a_full, aidx & 1u, abort_flag, fault, 3)) { ok = false; break; }
+                    ++aidx;
+                    cur_i = tp.x;
+                    tc_fence_after();
+                }
+                const int b = (int)(local % kAccBufs);
+                const uint32_t tph = (local / kAccBufs) & 1u;
+                if (!mbar_wait_fast(&tempty[b], tph ^ 1u, abort_flag, fault, 4)) { ok = false; break; }
+                const int q = (int)(local % (uint32_t)nslots);
+                const uint32_t ph = (local / (uint32_t)nslots) & 1u;
+                if (!mbar_wait_fast(&b_full[q], ph, abort_flag, fault, 5)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols);
-                for (int kc = 0; kc < kchunks; ++kc, ++it) {
-                    const int s = it % kNS;
-                    const uint32_t ph = (it / kNS) & 1u;
-                    if (!mbar_wait(&full[s], ph, abort_flag, fault, 3)) { ok = false; break; }
-                    tc_fence_after();
-                    const uint32_t a0 = smem_u32(sm + GramSmem::stages + s * kStageBytes);
-                    const uint64_t adesc = sw128_desc(a0), bdesc = sw128_desc(a0 + kChunkBytes);
+                const uint32_t a0 = smem_u32(sm + GramSmem::a_tile);
+                const uint32_t b0 = smem_u32(sm + GramSmem::b_ring + q * slot_bytes);
+                for (int kc = 0; kc < kchunks; ++kc) {
+                    const uint64_t adesc = sw128_desc(a0 + kc * kChunkBytes);
+                    const uint64_t bdesc = sw128_desc(b0 + kc * kChunkBytes);
 #pragma unroll
                     for (int k = 0; k < kChunkK / 16; ++k)
                         umma_bf16(tacc, adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), kIdesc,
                                   (kc | k) != 0 ? 1u : 0u);
-                    umma_commit(&empty[s]);
-                    any = true;
                 }
-                if (!ok) break;
+                any = true;
+                umma_commit(&b_empty[q]);
                 umma_commit(&tfull[b]);
+                // release the A tile after its last item's MMAs
+                if (pf.q0.x != cur_i) umma_commit(a_empty);  // pf.q0 is item w + 1 (or -1 past the end)
             }
             if (!ok && any) {
                 // wait (bounded) for the MMAs already issued before tensor memory is freed
@@ -316,83 +406,123 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         }
     } else {
         // ---------------- epilogue warps
-        const int ew = warp - 2;                       // 0..3
+        // Candidate test per element: -2 g + u_j <= W_i, where u_j = n_j - a_j^2 - q_j
+        // and W_i = A_i^2 + q_i - n_i + 2 A_i amax_J (+ rounding slack), A_i = eps' + a_i.
+        // Replacing a_j by the column tile's max a only widens the test, so it still
+        // admits every pair with (eps' + a_i + a_j)^2 + q_i + q_j >= D~.
+        const int ew = warp - 2;
+        const int grp = ew / kGroupWarps;              // this group takes items wbeg + grp, + kEpiGroups, ...
         const int sub = warp & 3;                      // TMEM sub-partition this warp may access
-        float4* colinfo = (float4*)(sm + GramSmem::colinfo) + ew * kTile;
-        uint32_t local = 0;
-        for (unsigned long long w = blockIdx.x; w < npairs; w += gridDim.x, ++local) {
-            const int2 tp = pairs[w];
-            const int b = local & 1;
-            const uint32_t tph = (local >> 1) & 1u;
-            // column data of tile J (norm, error radius, Gram error term)
-            for (int k = lane; k < kTile; k += 32) colinfo[k] = rowinfo[(int64_t)tp.y * kTile + k];
-            const int r = sub * 32 + lane;
+        const int cg = (ew % kGroupWarps) >> 2;        // column group: columns [kEpiCols cg, +kEpiCols)
+        float* colu = (float*)(sm + GramSmem::colinfo) + ew * kEpiCols;
+        const int r = sub * 32 + lane;
+        PairPrefetch pf;
+        pf.init(pairs, wbeg + grp, wend, kEpiGroups);
+        // row / column data of the current item, loaded one item ahead
+        int2 tp = pf.next(wbeg + grp);
+        float2 uc = make_float2(0.f, 0.f);
+        float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 tj = make_float2(0.f, 0.f);
+        if (wbeg + grp < wend) {
+            uc = reinterpret_cast<const float2*>(ucol)[((int64_t)tp.y * kTile + cg * kEpiCols) / 2 + lane];
+            ri = rowinfo[(int64_t)tp.x * kTile + r];
+            tj = tileinfo[tp.y];
+        }
+        uint32_t local = (uint32_t)grp;
+        for (unsigned long long w = wbeg + grp; w < wend; w += kEpiGroups, local += kEpiGroups) {
+            const int b = (int)(local % kAccBufs);
+            const uint32_t tph = (local / kAccBufs) & 1u;
+            const int64_t j0 = (int64_t)tp.y * kTile + cg * kEpiCols;
             const int64_t gi = (int64_t)tp.x * kTile + r;
-            const float4 ri = rowinfo[gi];
-            const float Ai = eps_p + ri.y;
+            const bool diag = tp.x == tp.y;
+            reinterpret_cast<float2*>(colu)[lane] = uc;
+            const float A = eps_p + ri.y;
+            const float AA = A * A, cross = 2.f * A * tj.x;
+            const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
+            // issue the next item's loads now; they complete while this item is tested
+            const int2 tpn = pf.next(w + kEpiGroups);
+            if (w + kEpiGroups < wend) {
+                uc = reinterpret_cast<const float2*>(ucol)[((int64_t)tpn.y * kTile + cg * kEpiCols) / 2 + lane];
+                ri = rowinfo[(int64_t)tpn.x * kTile + r];
+                tj = tileinfo[tpn.y];
+            }
+            tp = tpn;
             __syncwarp();
-            // lane 0 waits (bounded); the others then observe the completed phase
-            bool ready = (lane == 0) ? mbar_wait(&tfull[b], tph, abort_flag, fault, 4) : false;
-            ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
-            if (!ready) break;
-            while (!mbar_try_wait(&tfull[b], tph)) {
+            // fast path: the accumulator is usually ready; otherwise lane 0 waits (bounded)
+            if (!__all_sync(0xffffffffu, mbar_try_wait(&tfull[b], tph))) {
+                bool ready = (lane == 0) ? mbar_wait(&tfull[b], tph, abort_flag, fault, 6) : false;
+                ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+                if (!ready) break;
+                while (!mbar_try_wait(&tfull[b], tph)) {
+                }
             }
             tc_fence_after();
-            uint32_t masks[kAccCols / 32];
-#pragma unroll
-            for (int ch = 0; ch < kAccCols / 32; ++ch) {
+            const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) + (uint32_t)(b * kAccCols + cg * kEpiCols);
+            for (int ch = 0; ch < kEpiCols / 32; ++ch) {
                 float g[32];
-                tmem_ld32(tmem_base + ((uint32_t)(sub * 32) << 16) + (uint32_t)(b * kAccCols + ch * 32), g);
-                uint32_t m = 0;
-#pragma unroll
-                for (int t = 0; t < 32; ++t) {
-                    const float4 cj = colinfo[ch * 32 + t];
-                    const float dd = fmaf(-2.f, g[t], ri.x + cj.x);
-                    const float s = Ai + cj.y;
-                    const float rhs = fmaf(s, s, ri.z + cj.z) * kappa;
-                    m |= (dd <= rhs ? 1u : 0u) << t;
+                tmem_ld32(taddr + ch * 32, g);
+                if (ch == kEpiCols / 32 - 1) {
+                    // accumulator slice read: hand it back to the MMA warp
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[b]);
                 }
-                masks[ch] = m;
-            }
-            // accumulator fully read: hand it back to the MMA warp
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty[b]);
-            // append candidates (gi < gj inside a diagonal tile; padding rows excluded)
+                // most rows have no candidate: test the minimum first
+                float mn = INFINITY;
 #pragma unroll
-            for (int ch = 0; ch < kAccCols / 32; ++ch) {
-                uint32_t m = masks[ch];
-                const int64_t j0 = (int64_t)tp.y * kTile + ch * 32;
+                for (int t4 = 0; t4 < 8; ++t4) {
+                    const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
+                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 0], u4.x));
+                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 1], u4.y));
+                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 2], u4.z));
+                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 3], u4.w));
+                }
+                const bool mine = mn <= Wi;
+                if (!__any_sync(0xffffffffu, mine)) continue;
+                uint32_t m = 0;
+                if (mine) {
+#pragma unroll
+                    for (int t4 = 0; t4 < 8; ++t4) {
+                        const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
+                        m |= (fmaf(-2.f, g[4 * t4 + 0], u4.x) <= Wi ? 1u : 0u) << (4 * t4 + 0);
+                        m |= (fmaf(-2.f, g[4 * t4 + 1], u4.y) <= Wi ? 1u : 0u) << (4 * t4 + 1);
+                        m |= (fmaf(-2.f, g[4 * t4 + 2], u4.z) <= Wi ? 1u : 0u) << (4 * t4 + 2);
+                        m |= (fmaf(-2.f, g[4 * t4 + 3], u4.w) <= Wi ? 1u : 0u) << (4 * t4 + 3);
+                    }
+                }
+                const int64_t jc = j0 + ch * 32;
+                // padding rows / columns and, inside a diagonal tile, j <= i excluded
                 if (gi >= n) m = 0;
-                if (j0 + 32 > n) {
-                    int64_t lim = n - j0;
+                if (jc + 32 > n) {
+                    const int64_t lim = n - jc;
                     m &= lim <= 0 ? 0u : (lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u));
                 }
-                if (tp.x == tp.y) {
-                    // keep columns j with j0 + t > gi
-                    int64_t first = gi - j0 + 1;
+                if (diag) {
+                    const int64_t first = gi - jc + 1;
                     m &= first <= 0 ? 0xffffffffu : (first >= 32 ? 0u : ~((1u << first) - 1u));
                 }
                 const int cnt = __popc(m);
                 int incl = cnt;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= o) incl += t;
                 }
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
-                if (total == 0) continue;
-                unsigned long long base = 0;
-                if (lane == 31) base = atomicAdd(cand_count, (unsigned long long)total);
-                base = __shfl_sync(0xffffffffu, base, 31);
-                unsigned long long pos = base + (unsigned long long)(incl - cnt);
-                while (m) {
-                    const int t = __ffs(m) - 1;
-                    m &= m - 1;
-                    if (pos < cand_cap) cand[pos] = make_uint2((uint32_t)gi, (uint32_t)(j0 + t));
-                    ++pos;
+                if (total > 0) {
+                    unsigned long long base = 0;
+                    if (lane == 31) base = atomicAdd(cand_count, (unsigned long long)total);
+                    base = __shfl_sync(0xffffffffu, base, 31);
+                    unsigned long long pos = base + (unsigned long long)(incl - cnt);
+                    while (m) {
+                        const int t = __ffs(m) - 1;
+                        m &= m - 1;
+                        if (pos < cand_cap) cand[pos] = make_uint2((uint32_t)gi, (uint32_t)(jc + t));
+                        ++pos;
+                    }
                 }
             }
+            __syncwarp();
         }
     }
 
@@ -523,8 +653,33 @@ __global__ void k_to_bf16(const float* __restrict__ Xs, int64_t n, int64_t n_pad
             const float a = (sqrtf(res) + u * sqrtf(xc)) * grow * grow + 1e-30f;
             // q >= Gram error share of this row: gamma * ||x~||^2 (upper bound on the norm)
             const float q = gamma * nrm * grow;
-            rowinfo[r] = make_float4(nrm, a, q, 0.f);
+            rowinfo[r] = make_float4(nrm, a, q, nrm - a * a - q);
         }
+    }
+}
+
+// Per tile: max error radius a and max of (n + a^2 + q) over its rows, plus the
+// column array u = n - a^2 - q used by the candidate test.
+__global__ void k_tile_info(const float4* __restrict__ rowinfo, int64_t T, float* __restrict__ ucol,
+                            float2* __restrict__ tileinfo)
+{
+    const int64_t t = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ float s_a[4], s_n[4];
+    const float4 ri = rowinfo[t * kTile + threadIdx.x];
+    ucol[t * kTile + threadIdx.x] = ri.w;
+    float amax = ri.y, nmax = ri.x + ri.y * ri.y + ri.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+        nmax = fmaxf(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+    }
+    if (lane == 0) { s_a[warp] = amax; s_n[warp] = nmax; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float grow = 1.0f + 1.0f / (1 << 20);
+        tileinfo[t] = make_float2(fmaxf(fmaxf(s_a[0], s_a[1]), fmaxf(s_a[2], s_a[3])) * grow,
+                                  fmaxf(fmaxf(s_n[0], s_n[1]), fmaxf(s_n[2], s_n[3])) * grow);
     }
 }
 
@@ -548,7 +703,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode()
 
 }  // namespace
 
-bool bf16_supported(int d) { return d >= 1 && d <= 1024; }
+bool bf16_supported(int d) { return d >= 1 && d <= kMaxDp; }
 
 void prepare_bf16(rnng_ctx* c, Layout& L)
 {
@@ -556,9 +711,12 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     const int d = L.d;
     const int dp = (int)ceil_div(d, kChunkK) * kChunkK;
     c->xb_sorted.reserve(sizeof(__nv_bfloat16) * (size_t)L.n_pad * dp);
-    c->norms.reserve(sizeof(float4) * (size_t)L.n_pad + sizeof(double) * d + sizeof(float) * d + 64);
+    c->norms.reserve(sizeof(float4) * (size_t)L.n_pad + sizeof(float) * (size_t)L.n_pad +
+                     sizeof(float2) * (size_t)L.T + sizeof(double) * d + sizeof(float) * d + 64);
     float4* rowinfo = c->norms.as<float4>();
-    double* sums = (double*)(rowinfo + L.n_pad);
+    float* ucol = (float*)(rowinfo + L.n_pad);
+    float2* tileinfo = (float2*)(ucol + L.n_pad);
+    double* sums = (double*)(tileinfo + L.T + (L.T & 1));
     float* shift = (float*)(sums + d);
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     k_colsum<<<std::min<int64_t>(std::max<int64_t>(L.n / 256, 1), (int64_t)c->num_sms * 4), 128, 0, s>>>(L.Xs, L.n,
@@ -570,7 +728,10 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     const double gamma = (double)dp * std::ldexp(1.0, -19) + (double)(d + 2) * u + 8.0 * u;
     k_to_bf16<<<std::min<int64_t>(ceil_div(L.n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0, s>>>(
         L.Xs, L.n, L.n_pad, d, dp, shift, (float)gamma, c->xb_sorted.as<__nv_bfloat16>(), rowinfo);
+    k_tile_info<<<(unsigned)L.T, kTile, 0, s>>>(rowinfo, L.T, ucol, tileinfo);
     RNNG_CUDA(cudaGetLastError());
+    c->bf16_ucol = ucol;
+    c->bf16_tileinfo = tileinfo;
 
     static_assert(sizeof(CUtensorMap) == sizeof(c->tmap), "tensor map storage");
     c->bf16_dp = dp;
@@ -602,15 +763,16 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
-    const int grid = (int)std::max<unsigned long long>(
-        1, std::min<unsigned long long>(L.tile_pairs, (unsigned long long)c->num_sms));
-    const float kappa = 1.f + 1.0f / (1 << 18);
+    const int grid = L.sched_G;
+    RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
+    const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
     for (int attempt = 0;; ++attempt) {
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         k_gram_bf16<<<grid, kGramThreads, smem, s>>>(tm, L.pairs, L.d_tile_pairs, L.tile_pairs, kchunks,
-                                                      (const float4*)c->bf16_rowinfo, L.n, c->bf16_eps_p, kappa,
-                                                      c->cand.as<uint2>(), cnt, ccap, c->fault_word);
+                                                      (const float4*)c->bf16_rowinfo, (const float*)c->bf16_ucol,
+                                                      (const float2*)c->bf16_tileinfo, L.n, c->bf16_eps_p, kappa,
+                                                      c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
         RNNG_CUDA(cudaGetLastError());
         unsigned long long got = 0;
         RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
@@ -627,6 +789,7 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         ccap = got + got / 8 + 1024;
         c->stats.retries++;
     }
+    RNNG_CUDA(cudaEventRecord(c->ev[8], s));
     const unsigned long long ncand = (unsigned long long)c->last_candidates;
     const int rgrid = (int)std::max<unsigned long long>(
         1, std::min<unsigned long long>((ncand + 255) / 256, (unsigned long long)c->num_sms * 8));

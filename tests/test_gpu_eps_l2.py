@@ -88,7 +88,7 @@ def test_integer_descriptors_30k(ctx, orc, mode):
 def test_modes_agree_and_fp64_error(ctx):
     from rnng_gb300 import synth
     x = synth.zipf_mixture(n=40000, d=32, k=256, seed=21)
-    r = np.float32(3.0)
+    r = np.float32(4.5)
     a = ctx.eps_graph_l2(x, r, mode="fp32")
     b = ctx.eps_graph_l2(x, r, mode="bf16")
     assert same(a, b) and a[0].size > 0

@@ -1,0 +1,328 @@
+"""Benchmark: epsilon-graph edges/s on 1,000,000 x 128 float32 integer descriptors.
+
+One step = one call of the epsilon-graph hot path (rnng_eps_graph_l2) over the whole
+point set: partition, tile covers and pruning, BF16 tensor-core Gram tiles with the
+exact FP32 recheck, compaction to the final (u, v, w) edge list.  The reported value
+is edges/s of the BF16 form with the points already resident in HBM; the plain FP32
+form (same partition and pruning, every pair evaluated with the sequential FP32 L2)
+is timed beside it, and both produce the identical edge set.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the CPU restatement of RNNG's path is timed on the host cores
+(see cpu_leg below) on a bounded sample of the same workload.  Under torchrun (N > 1)
+every rank runs an independent replica on its own GPU (the path is not sharded).
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "eps-graph edges/s, 1M×128 f32: BF16-TC+recheck vs plain FP32 GPU, same edges"
+UNIT = "edges/s"
+N_POINTS, DIM = 1_000_000, 128
+
+
+def workload():
+    from rnng_gb300 import synth
+    return synth.descriptor(n=N_POINTS, d=DIM), synth.EPS_K2
+
+
+def config(extra=None):
+    from rnng_gb300 import synth
+    c = {"workload": "k2-descriptors-1Mx128-f32", "points": N_POINTS, "dim": DIM,
+         "radius": float(synth.EPS_K2), "radius_hex": hex(int(np.float32(synth.EPS_K2).view(np.uint32))),
+         "clusters": 1000, "values": "integers 0..255 stored as float32",
+         "l2_flush": "not needed: inputs (512 MB) larger than L2 (129 MB)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ----------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU leg
+
+def cpu_leg(x, radius, budget_s: float = 20.0, threads: int | None = None) -> dict:
+    """Times the CPU restatement of RNNG's path on a bounded sample of the workload.
+
+    The oracle evaluates the reference predicate (sequential FP32 L2 <= radius) for a
+    strided sample of query rows against all points; the measured time per pair
+    evaluation is scaled to the whole job (n (n-1) / 2 pair evaluations for the
+    |E| edges the GPU found) to give edges/s.
+    """
+    import oracle
+    oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.num_threads()
+    n = x.shape[0]
+    # calibrate the sample to about budget_s of work
+    rows = 64
+    t0 = time.perf_counter()
+    oracle.cross_l2(x, x[:: n // rows][:rows], radius)
+    t_cal = time.perf_counter() - t0
+    rows = int(max(64, min(20000, rows * budget_s / max(t_cal, 1e-3))))
+    idx = np.linspace(0, n - 1, rows).astype(np.int64)
+    t0 = time.perf_counter()
+    u, v, w = oracle.cross_l2(x, x[idx], radius)
+    dt = time.perf_counter() - t0
+    pair_time = dt / (rows * n)
+    # every sampled row also matches itself (distance 0)
+    mean_degree = (u.size - rows) / rows
+    return {"pair_time_s": pair_time, "cores": cores, "rows": rows, "seconds": dt, "mean_degree": mean_degree}
+
+
+def cpu_value(leg: dict, edges: int, n: int) -> float:
+    return edges / (leg["pair_time_s"] * n * (n - 1) / 2)
+
+
+# ----------------------------------------------------------------------------- main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp32-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+
+    import rnng_gb300
+    x, radius = workload()
+    n, d = x.shape
+    ctx = rnng_gb300.Context(local)
+    xd = torch.from_numpy(x).to(f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=f"cuda:{local}")
+    flags_dev = rnng_gb300.INPUT_DEVICE | rnng_gb300.OUTPUT_DEVICE
+
+    def step(mode):
+        e = ctx.eps_graph_l2_raw(xd.data_ptr(), None, n, d, radius, mode, flags_dev)
+        return e.count
+
+    # ---- BF16 tensor-core form: warm-up, then K timed steps on the library's stream
+    for _ in range(args.warmup):
+        edges = step(1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gram_ms, launches, tile_pairs, cands = [], [], [], []
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        edges = step(1)
+        st = ctx.stats()
+        gram_ms.append(st["ms_gram"])
+        launches.append(st["kernel_launches"])
+        tile_pairs.append(st["tile_pairs"])
+        cands.append(st["candidates"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * edges * args.steps / (ms / 1e3)
+    last = ctx.stats()
+
+    # ---- plain FP32 form (same partition and pruning), a few steps
+    fp32 = None
+    if args.fp32_steps > 0:
+        step(0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp32_steps):
+            edges32 = step(0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1) / args.fp32_steps
+        assert edges32 == edges, "FP32 and BF16 forms found different edge counts"
+        fp32 = {"value": edges / (ms32 / 1e3), "ms_per_step": ms32,
+                "bf16_speedup": ms32 / ms_step}
+
+    # ---- end to end through the C ABI with host buffers (pinned input, host result)
+    xh = torch.from_numpy(x).pin_memory()
+    ctx.eps_graph_l2_raw(xh.data_ptr(), None, n, d, radius, 1, 0)
+    t_e2e = []
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = ctx.eps_graph_l2_raw(xh.data_ptr(), None, n, d, radius, 1, 0)
+        t_e2e.append(time.perf_counter() - t0)
+        assert e.count == edges
+    e2e_s = statistics.median(t_e2e)
+    e2e = {"value": world * edges / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(n * d * 4),
+           "d2h_bytes_per_step": int(edges * (8 + 8 + 4)), "ms_per_step": e2e_s * 1e3}
+
+    # ---- roofline of the dominant kernel (tcgen05 Gram tiles)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["bf16_tflops_sustained"]), "of measured (sustained bf16)"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 1900.0, "of fallback"
+    pairs = last["pairs_evaluated"]
+    g_ms = statistics.median(gram_ms)
+    achieved = 2.0 * d * pairs / (g_ms / 1e3) / 1e12
+    traffic = read_profile_traffic()
+    roofline = {"bound": "tensor", "kernel": "k_gram_bf16", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                "flops_per_launch": 2.0 * d * pairs, "ms_per_launch": g_ms,
+                "algorithmic": "2*d flops per evaluated point pair (x.y), pairs = surviving tile pairs * 128 * 128"}
+
+    # ---- CPU baseline (rank 0 only)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        leg = cpu_leg(x, radius)
+        cpu = {"value": cpu_value(leg, edges, n), "unit": UNIT, "cores": leg["cores"], "kind": "port",
+               "sample": f"{leg['rows']} strided query rows x all {n} points with the oracle's reference "
+                         f"predicate ({leg['seconds']:.1f} s), time per pair scaled to n(n-1)/2 pairs"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
+                "config": config({"parallelism": "replicas" if world > 1 else "single-gpu",
+                                  "edges": int(edges), "tile_pairs": int(last["tile_pairs"]),
+                                  "tile_pairs_all": int(last["tile_pairs_all"]),
+                                  "candidates": int(last["candidates"]),
+                                  "stage_ms": {k: round(last[k], 3) for k in
+                                               ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles", "ms_recheck",
+                                                "ms_finalize")}}),
+                "fp32_direct": fp32, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "gpu_launches": int(sum(launches)), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    ctx.close()
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch of k_gram_bf16 from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_gram_bf16__k2_1Mx128.md")
+    try:
+        for ln in open(p):
+            if ln.startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args, world, rank):
+    """Reference arm: RNNG's CPU path restated by the oracle, timed on the host cores."""
+    if rank != 0:
+        return
+    x, radius = workload()
+    n = x.shape[0]
+    vals = []
+    for i in range(args.warmup + args.steps):
+        leg = cpu_leg(x, radius, budget_s=10.0)
+        # edges of the whole job estimated from the sampled rows' mean degree
+        edges = n * leg["mean_degree"] / 2
+        if i >= args.warmup:
+            vals.append(cpu_value(leg, edges, n))
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
+            "config": config(), "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": leg["cores"], "kind": "port",
+                             "sample": f"{leg['rows']} strided query rows x all {n} points per step"}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

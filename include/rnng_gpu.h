@@ -11,11 +11,11 @@
  *     Nothing throws across this boundary.  rnng_last_error() gives the message.
  *   - Plain pointers and sizes only.  Pointers are host memory unless the call's
  *     flags say RNNG_INPUT_DEVICE (inputs) / RNNG_OUTPUT_DEVICE (outputs).
- *   - Results live in library-owned buffers.  With RNNG_OUTPUT_DEVICE they are
- *     device allocations that stay valid until rnng_edges_free / rnng_simplices_free.
- *     Otherwise they are host arrays in the context's pinned staging memory, valid
- *     until the next call on the same context (copy them to keep them); freeing
- *     them is a no-op.
+ *   - Results live in library-owned buffers of the context: device arrays with
+ *     RNNG_OUTPUT_DEVICE, otherwise host arrays in the context's pinned staging
+ *     memory.  Either way they stay valid until the next call on the same context
+ *     (copy them to keep them); rnng_edges_free / rnng_simplices_free on them is a
+ *     no-op, so steady-state calls allocate nothing.
  *   - All work of a context is ordered on the context's CUDA stream.  One context
  *     per host thread; calls on one context must not overlap.
  *   - Point ids are int64 (RNNG's Index, include/utils.h:24); distances are float
@@ -63,8 +63,8 @@ typedef struct rnng_edges {
     int64_t* u;
     int64_t* v;
     float* w;
-    int on_device; /* 1: u, v, w are device pointers owned by the caller */
-    int staged;    /* 1: host arrays in the context's staging memory (not freed by rnng_edges_free) */
+    int on_device; /* 1: u, v, w are device pointers */
+    int staged;    /* 1: arrays owned by the context (not freed by rnng_edges_free) */
 } rnng_edges;
 
 /* A filtration: simplex ids (RNNG's Simplex encoding, include/simplex.hpp:5-19) and values. */
@@ -89,6 +89,7 @@ typedef struct rnng_stats {
     int64_t retries;        /* edge-buffer regrowths */
     int64_t simplices;      /* Rips: simplices emitted */
     int64_t kernel_launches;/* kernels launched by the call */
+    double ms_gram;         /* BF16 mode: device time of the tensor-core Gram kernel */
 } rnng_stats;
 
 /* Context ---------------------------------------------------------------------------------

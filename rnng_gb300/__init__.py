@@ -60,7 +60,8 @@ class Stats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("ms_total", "ms_h2d", "ms_partition", "ms_sort", "ms_bounds",
                                                  "ms_prune", "ms_tiles", "ms_recheck", "ms_finalize", "ms_d2h")] + \
                [(k, ctypes.c_int64) for k in ("num_cells", "super_pairs", "tile_pairs", "tile_pairs_all", "pairs_evaluated",
-                                              "candidates", "edges", "retries", "simplices", "kernel_launches")]
+                                              "candidates", "edges", "retries", "simplices", "kernel_launches")] + \
+               [("ms_gram", ctypes.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -83,15 +83,12 @@ void deliver_edges(rnng_ctx* c, const int64_t* du, const int64_t* dv, const floa
     out->count = m;
     size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1), bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
     if (flags & RNNG_OUTPUT_DEVICE) {
+        // the context's own result buffers, valid until the next call
         out->on_device = 1;
-        RNNG_CUDA(cudaMalloc(&out->u, bi));
-        RNNG_CUDA(cudaMalloc(&out->v, bi));
-        RNNG_CUDA(cudaMalloc(&out->w, bf));
-        if (m) {
-            RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, c->stream));
-            RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, c->stream));
-            RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToDevice, c->stream));
-        }
+        out->staged = 1;
+        out->u = const_cast<int64_t*>(du);
+        out->v = const_cast<int64_t*>(dv);
+        out->w = const_cast<float*>(dw);
     } else {
         out->staged = 1;
         char* h = (char*)stage(c, c->host_stage, 2 * bi + bf);
@@ -233,6 +230,8 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         if (mode == RNNG_MODE_BF16_RECHECK)
             RNNG_REQUIRE(bf16_supported((int)d), RNNG_ERR_UNSUPPORTED, "BF16 mode supports d <= 256");
         c->stats = rnng_stats{};
+        c->launches = 0;
+        c->gram_ms = 0.0;
         cudaStream_t s = c->stream;
         RNNG_CUDA(cudaEventRecord(c->ev[0], s));
         const float* dX = upload_f32(c, c->x_in, X, n * d, flags);
@@ -241,7 +240,10 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         if (n < 2 || radius < 0.f) {
             // no pair can be an edge (a negative radius admits no distance)
             RNNG_CUDA(cudaEventRecord(c->ev[2], s));
-            deliver_edges(c, nullptr, nullptr, nullptr, 0, flags, out);
+            c->out_u.reserve(8);
+        c->out_v.reserve(8);
+        c->out_w.reserve(8);
+        deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), 0, flags, out);
             RNNG_CUDA(cudaStreamSynchronize(s));
             return;
         }
@@ -291,13 +293,15 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         st.pairs_evaluated = (int64_t)L.tile_pairs * kTile * kTile;
         st.edges = m;
         st.candidates = c->last_candidates;
+        st.kernel_launches = c->launches;
+        st.ms_gram = c->gram_ms;
     });
 }
 
 int rnng_edges_free(rnng_edges* e)
 {
     if (!e) return RNNG_ERR_INVALID;
-    if (e->on_device) {
+    if (e->on_device && !e->staged) {
         cudaFree(e->u);
         cudaFree(e->v);
         cudaFree(e->w);
@@ -309,7 +313,7 @@ int rnng_edges_free(rnng_edges* e)
 int rnng_simplices_free(rnng_simplices* s)
 {
     if (!s) return RNNG_ERR_INVALID;
-    if (s->on_device) {
+    if (s->on_device && !s->staged) {
         cudaFree(s->id);
         cudaFree(s->value);
     }

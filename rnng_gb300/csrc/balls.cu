@@ -487,7 +487,7 @@ void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchil
                   int ncells, int32_t* rank)
 {
     const size_t smem = sizeof(float) * kChainMax * (kChainMax - 1) / 2;
-    k_chain_leaves<<<ncells, 256, smem, c->stream>>>(lm_rows, d, nchild, child_off, rank);
+    k_chain_leaves<<<ncells, 256, smem, c->stream>>>(lm_rows, d, nchild, child_off, rank); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 
@@ -500,10 +500,10 @@ void build_covers(rnng_ctx* c, Layout& L)
     c->super_lo.reserve(sizeof(float) * (size_t)L.S * kBalls * L.d);  // super ball centres
     c->super_hi.reserve(sizeof(float) * (size_t)L.S * kBalls);        // super ball radii
     c->pivots.reserve(sizeof(float) * (size_t)L.S * kSuper * kBalls * L.d);  // compaction workspace
-    k_tile_balls<<<(unsigned)L.T, 256, 0, s>>>(L.Xs, L.n, L.d, grow, c->tile_lo.as<float>(), c->tile_hi.as<float>());
+    k_tile_balls<<<(unsigned)L.T, 256, 0, s>>>(L.Xs, L.n, L.d, grow, c->tile_lo.as<float>(), c->tile_hi.as<float>()); ++c->launches;
     k_super_balls<<<(unsigned)L.S, 256, 0, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d, grow,
                                                 c->pivots.as<float>(), c->super_lo.as<float>(),
-                                                c->super_hi.as<float>());
+                                                c->super_hi.as<float>()); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 
@@ -523,14 +523,14 @@ void prune_covers(rnng_ctx* c, Layout& L)
     RNNG_CUDA(cudaMemsetAsync(bitmap, 0, sizeof(uint32_t) * (size_t)words, s));
     dim3 g1((unsigned)ceil_div(NB, kDRows), (unsigned)ceil_div(NB, kDCols));
     k_super_close<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), NB, L.d, eps_p, shrink, bitmap,
-                                     L.S);
+                                     L.S); ++c->launches;
     unsigned long long sup_cap = std::max<unsigned long long>(4096, (unsigned long long)L.S * 64);
     sup_cap = std::min<unsigned long long>(sup_cap, (unsigned long long)L.S * (L.S + 1) / 2);
     for (int attempt = 0; attempt < 3; ++attempt) {
         c->super_list.reserve(sizeof(int2) * sup_cap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         k_bitmap_pairs<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(words, 256), (int64_t)c->num_sms * 8)),
-                         256, 0, s>>>(bitmap, L.S, c->super_list.as<int2>(), cnt, sup_cap);
+                         256, 0, s>>>(bitmap, L.S, c->super_list.as<int2>(), cnt, sup_cap); ++c->launches;
         unsigned long long got = 0;
         RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
@@ -547,7 +547,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
         1, std::min<unsigned long long>(L.super_pairs, (unsigned long long)c->num_sms * 16));
     k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
                                       c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(), cnt + 1,
-                                      tile_cap);
+                                      tile_cap); ++c->launches;
     unsigned long long got = 0;
     RNNG_CUDA(cudaMemcpyAsync(&got, cnt + 1, sizeof(got), cudaMemcpyDeviceToHost, s));
     RNNG_CUDA(cudaStreamSynchronize(s));
@@ -576,13 +576,13 @@ void schedule_pairs(rnng_ctx* c, Layout& L, int G)
     uint64_t* k0 = c->aux6.as<uint64_t>();
     uint64_t* k1 = k0 + m;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
-    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, G, k0);
+    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, G, k0); ++c->launches;
     size_t tmp = 0;
     RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, 64, s));
     c->cub_tmp.reserve(tmp);
-    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, 64, s));
-    k_schedule_unpack<<<grid, 256, 0, s>>>(k1, m, L.pairs, starts);
-    k_schedule_fix<<<1, 1, 0, s>>>(starts, G);
+    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, 64, s)); c->launches += cub_sort_kernels(m, 64);
+    k_schedule_unpack<<<grid, 256, 0, s>>>(k1, m, L.pairs, starts); ++c->launches;
+    k_schedule_fix<<<1, 1, 0, s>>>(starts, G); ++c->launches;
     RNNG_CUDA(cudaStreamSynchronize(s));  // init lifetime
 }
 

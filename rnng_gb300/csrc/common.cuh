@@ -92,6 +92,8 @@ struct rnng_ctx {
     void* bf16_tileinfo = nullptr;
     float bf16_eps_p = 0.f;
     int* fault_word = nullptr;  // device error word written by kernels with bounded waits
+    int64_t launches = 0;       // kernels launched by the current call
+    double gram_ms = 0.0;       // device time of the Gram kernel launches of the current call
     cudaEvent_t ev[16] = {};
     bool have_events = false;
 };
@@ -106,6 +108,15 @@ inline void ensure_events(rnng_ctx* c)
 }
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Kernels one CUB radix sort launches: a single-tile kernel for small inputs,
+// otherwise histogram + exclusive sum + one onesweep pass per 8 key bits.
+inline int cub_sort_kernels(int64_t n, int bits)
+{
+    if (n <= 1) return 0;
+    if (n <= 4096) return 1;
+    return 2 + (bits + 7) / 8;
+}
 
 // Reference L2 (drivers/systolic.cpp:253-269): sequential difference-square-sum in
 // float without contraction, then a correctly rounded square root.  The explicit

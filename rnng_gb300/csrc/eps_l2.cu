@@ -238,7 +238,7 @@ void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t co
     RNNG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int)count, c->stream));
     c->cub_tmp.reserve(tmp);
     RNNG_CUDA(cudaMemsetAsync((void*)(in + count - 1), 0, sizeof(int32_t), c->stream));
-    RNNG_CUDA(cub::DeviceScan::ExclusiveSum(c->cub_tmp.ptr, tmp, in, out, (int)count, c->stream));
+    RNNG_CUDA(cub::DeviceScan::ExclusiveSum(c->cub_tmp.ptr, tmp, in, out, (int)count, c->stream)); c->launches += 2;
 }
 
 static int grid_for(rnng_ctx* c, int64_t work, int per_block, int waves = 8)
@@ -258,7 +258,7 @@ void sort_pairs_u64(rnng_ctx* c, uint64_t* keys_in, uint64_t* keys_out, int32_t*
                                               c->stream));
     c->cub_tmp.reserve(tmp);
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, keys_in, keys_out, vals_in, vals_out, (int)n, 0,
-                                              end_bit, c->stream));
+                                              end_bit, c->stream)); c->launches += cub_sort_kernels(n, end_bit);
 }
 
 static int bits_for(int64_t v)
@@ -287,7 +287,7 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     uint64_t* nkeys = c->keys.as<uint64_t>();       // keys of the next level, in current order
     int32_t* order = c->perm.as<int32_t>();          // current order: position -> input row
     int32_t* nvals = c->perm_alt.as<int32_t>();
-    k_iota_keys<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), (int64_t)c->num_sms * 8), 256, 0, s>>>(order, skeys, n);
+    k_iota_keys<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), (int64_t)c->num_sms * 8), 256, 0, s>>>(order, skeys, n); ++c->launches;
     int64_t ncells = 1;
     // per-cell scratch (cells never outnumber points)
     const int64_t cap = n + 2;
@@ -298,8 +298,8 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     int32_t* child_off = nchild + cap;
     int levels = 0;
     for (; levels < kMaxLevels; ++levels) {
-        k_cell_bounds<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(skeys, n, cstart, cend);
-        k_split_plan<<<(unsigned)ceil_div(ncells, 256), 256, 0, s>>>(cstart, cend, ncells, nchild);
+        k_cell_bounds<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(skeys, n, cstart, cend); ++c->launches;
+        k_split_plan<<<(unsigned)ceil_div(ncells, 256), 256, 0, s>>>(cstart, cend, ncells, nchild); ++c->launches;
         exclusive_scan_i32(c, nchild, child_off, ncells + 1);
         int32_t total = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, child_off + ncells, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -310,8 +310,8 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         c->aux5.reserve(sizeof(int32_t) * (size_t)total);
         int32_t* lm_idx = c->aux3.as<int32_t>();
         float* lm_rows = c->aux4.as<float>();
-        k_child_landmarks<<<(unsigned)ncells, 64, 0, s>>>(cstart, cend, nchild, child_off, ncells, order, lm_idx);
-        k_gather_rows<<<grid_for(c, (int64_t)total * d, 256), 256, 0, s>>>(dX, d, lm_idx, total, lm_rows);
+        k_child_landmarks<<<(unsigned)ncells, 64, 0, s>>>(cstart, cend, nchild, child_off, ncells, order, lm_idx); ++c->launches;
+        k_gather_rows<<<grid_for(c, (int64_t)total * d, 256), 256, 0, s>>>(dX, d, lm_idx, total, lm_rows); ++c->launches;
         // children ordered along a greedy nearest-neighbour chain of their landmarks
         chain_leaves(c, lm_rows, d, nchild, child_off, (int)ncells, c->aux5.as<int32_t>());
         launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, c->aux5.as<int32_t>(), nkeys, nvals);
@@ -325,7 +325,7 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     // ---- sorted points
     c->x_sorted.reserve(sizeof(float) * (size_t)L.n_pad * d);
     L.Xs = c->x_sorted.as<float>();
-    k_gather_sorted<<<grid_for(c, L.n_pad * d, 256), 256, 0, s>>>(dX, n, L.n_pad, d, order, L.Xs);
+    k_gather_sorted<<<grid_for(c, L.n_pad * d, 256), 256, 0, s>>>(dX, n, L.n_pad, d, order, L.Xs); ++c->launches;
     L.relerr = (float)((d + 16) * 1.1920928955078125e-07);  // (d+16) * 2^-23
     L.radius = radius;
     return L;
@@ -336,7 +336,7 @@ void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E)
     int grid = std::max(1, std::min<int>((int)std::min<unsigned long long>(L.tile_pairs, 1ull << 30),
                                          c->num_sms * 4));
     k_tiles_fp32<<<grid, 256, 0, c->stream>>>(L.Xs, L.n, L.d, L.pairs, L.d_tile_pairs, L.tile_pairs, L.radius, E.si,
-                                              E.sj, E.w, E.count, E.cap);
+                                              E.sj, E.w, E.count, E.cap); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 
@@ -344,7 +344,7 @@ void finalize_edges(rnng_ctx* c, const Layout& L, const int64_t* d_ids, const Ed
                     int64_t* v, float* w)
 {
     if (m == 0) return;
-    k_finalize_edges<<<grid_for(c, m, 256), 256, 0, c->stream>>>(E.si, E.sj, E.w, m, L.perm, d_ids, u, v, w);
+    k_finalize_edges<<<grid_for(c, m, 256), 256, 0, c->stream>>>(E.si, E.sj, E.w, m, L.perm, d_ids, u, v, w); ++c->launches;
 }
 
 }  // namespace rnng

@@ -720,15 +720,15 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     float* shift = (float*)(sums + d);
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     k_colsum<<<std::min<int64_t>(std::max<int64_t>(L.n / 256, 1), (int64_t)c->num_sms * 4), 128, 0, s>>>(L.Xs, L.n,
-                                                                                                           d, sums);
-    k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift);
+                                                                                                           d, sums); ++c->launches;
+    k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
     const double u = std::ldexp(1.0, -24);
     // tensor-core accumulation is modelled as at most 2^-19 relative error per
     // addition (truncating adds with fewer than 24 bits), far below its real error
     const double gamma = (double)dp * std::ldexp(1.0, -19) + (double)(d + 2) * u + 8.0 * u;
     k_to_bf16<<<std::min<int64_t>(ceil_div(L.n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0, s>>>(
-        L.Xs, L.n, L.n_pad, d, dp, shift, (float)gamma, c->xb_sorted.as<__nv_bfloat16>(), rowinfo);
-    k_tile_info<<<(unsigned)L.T, kTile, 0, s>>>(rowinfo, L.T, ucol, tileinfo);
+        L.Xs, L.n, L.n_pad, d, dp, shift, (float)gamma, c->xb_sorted.as<__nv_bfloat16>(), rowinfo); ++c->launches;
+    k_tile_info<<<(unsigned)L.T, kTile, 0, s>>>(rowinfo, L.T, ucol, tileinfo); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
     c->bf16_ucol = ucol;
     c->bf16_tileinfo = tileinfo;
@@ -769,14 +769,20 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     for (int attempt = 0;; ++attempt) {
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+        RNNG_CUDA(cudaEventRecord(c->ev[9], s));
         k_gram_bf16<<<grid, kGramThreads, smem, s>>>(tm, L.pairs, L.d_tile_pairs, L.tile_pairs, kchunks,
                                                       (const float4*)c->bf16_rowinfo, (const float*)c->bf16_ucol,
                                                       (const float2*)c->bf16_tileinfo, L.n, c->bf16_eps_p, kappa,
-                                                      c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+                                                      c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word); ++c->launches;
         RNNG_CUDA(cudaGetLastError());
+        RNNG_CUDA(cudaEventRecord(c->ev[10], s));
         unsigned long long got = 0;
         RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
+        {
+            float gms = 0.f;
+            if (cudaEventElapsedTime(&gms, c->ev[9], c->ev[10]) == cudaSuccess) c->gram_ms += gms;
+        }
         int fw = 0;
         RNNG_CUDA(cudaMemcpy(&fw, c->fault_word, sizeof(int), cudaMemcpyDeviceToHost));
         RNNG_REQUIRE(fw == FAULT_NONE, RNNG_ERR_DEVICE, "Gram kernel: bounded wait ran out (fault word set)");
@@ -794,7 +800,7 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     const int rgrid = (int)std::max<unsigned long long>(
         1, std::min<unsigned long long>((ncand + 255) / 256, (unsigned long long)c->num_sms * 8));
     k_recheck<<<rgrid, 256, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w, E.count,
-                                    E.cap);
+                                    E.cap); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 

@@ -48,21 +48,21 @@ void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m)
     int32_t* i1 = i0 + m;
     float* wtmp = (float*)(i1 + m);
     int grid = (int)std::min<int64_t>((m + 255) / 256, (int64_t)c->num_sms * 8);
-    k_iota<<<grid, 256, 0, s>>>(i0, m);
+    k_iota<<<grid, 256, 0, s>>>(i0, m); ++c->launches;
     size_t tmp = 0;
     // pass 1: by v (stable), pass 2: by u (stable) -> ordered by (u, v)
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s));
     c->cub_tmp.reserve(tmp);
-    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s));
-    k_gather<int64_t><<<grid, 256, 0, s>>>(u, i1, kbuf + m, m);
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s)); c->launches += cub_sort_kernels(m, 64);
+    k_gather<int64_t><<<grid, 256, 0, s>>>(u, i1, kbuf + m, m); ++c->launches;
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
     c->cub_tmp.reserve(tmp);
-    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
+    RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s)); c->launches += cub_sort_kernels(m, 64);
     // i0 = final order; u sorted = kbuf; v and w gathered
     RNNG_CUDA(cudaMemcpyAsync(u, kbuf, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
-    k_gather<int64_t><<<grid, 256, 0, s>>>(v, i0, kbuf, m);
+    k_gather<int64_t><<<grid, 256, 0, s>>>(v, i0, kbuf, m); ++c->launches;
     RNNG_CUDA(cudaMemcpyAsync(v, kbuf, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
-    k_gather<float><<<grid, 256, 0, s>>>(w, i0, wtmp, m);
+    k_gather<float><<<grid, 256, 0, s>>>(w, i0, wtmp, m); ++c->launches;
     RNNG_CUDA(cudaMemcpyAsync(w, wtmp, sizeof(float) * m, cudaMemcpyDeviceToDevice, s));
 }
 

@@ -95,7 +95,7 @@ void launch_assign(rnng_ctx* c, const float* X, const int32_t* rowmap, int64_t n
     const int64_t blocks = ceil_div(nrows, kDRows);
     if (blocks == 0) return;
     k_assign<<<(unsigned)blocks, 256, 0, c->stream>>>(X, rowmap, nrows, d, C, ncols, row_key, cell_off, col_rank,
-                                                      keys_out, vals_out);
+                                                      keys_out, vals_out); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 

@@ -36,7 +36,7 @@ MODES = {"fp32": 0, "bf16": 1}
 EXPORTS = [
     "rnng_ctx_create", "rnng_ctx_destroy", "rnng_last_error", "rnng_get_stats", "rnng_ctx_stream", "rnng_ctx_trim",
     "rnng_eps_graph_l2", "rnng_radius_query_l2", "rnng_voronoi_l2", "rnng_eps_graph_edit", "rnng_rips_l2",
-    "rnng_graph_finalize", "rnng_edges_free", "rnng_simplices_free",
+    "rnng_graph_finalize", "rnng_edges_free", "rnng_simplices_free", "rnng_eps_graph_l2_static",
 ]
 
 
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rnng_graph_finalize.argtypes = [vp, ctypes.POINTER(Edges), i64, u32, ctypes.POINTER(Edges)]
     L.rnng_edges_free.argtypes = [ctypes.POINTER(Edges)]
     L.rnng_simplices_free.argtypes = [ctypes.POINTER(Simplices)]
+    L.rnng_eps_graph_l2_static.argtypes = [vp, vp, i64, i64, f32, vp, vp, vp, i64, ctypes.POINTER(i64), vp]
     _lib = L
     return L
 

@@ -54,6 +54,7 @@ def lib() -> ctypes.CDLL:
         L.orc_rips.restype = ctypes.c_int64
         L.orc_rips.argtypes = [ctypes.c_int64, _i64p, _i64p, _f32p, ctypes.c_int64, ctypes.c_int,
                                ctypes.POINTER(_i64p), ctypes.POINTER(_f32p)]
+        L.orc_voronoi.argtypes = [_f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int64, _i64p, _f32p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -129,6 +130,16 @@ def eps_graph_edit(atoms: np.ndarray, offsets: np.ndarray, eps, rows: tuple[int,
                                    ctypes.c_float(eps), r0, r1, ctypes.byref(pu), ctypes.byref(pv),
                                    ctypes.byref(pw))
     return _edges(cnt, pu, pv, pw)
+
+
+def voronoi(X: np.ndarray, C: np.ndarray):
+    X = np.ascontiguousarray(X, np.float32)
+    C = np.ascontiguousarray(C, np.float32)
+    cell = np.zeros(X.shape[0], np.int64)
+    dist = np.zeros(X.shape[0], np.float32)
+    lib().orc_voronoi(X.ctypes.data_as(_f32p), X.shape[0], C.ctypes.data_as(_f32p), C.shape[0], X.shape[1],
+                      cell.ctypes.data_as(_i64p), dist.ctypes.data_as(_f32p))
+    return cell, dist
 
 
 def binom(n: int, k: int) -> int:

@@ -233,6 +233,27 @@ int64_t orc_eps_graph_edit(const uint8_t* atoms, const int64_t* offsets, int64_t
     return total;
 }
 
+/* Nearest centre per point as VoronoiDiagram::VoronoiDiagram (include/point.hpp:
+ * 537-559): distance(center, point), `dist <= best` over centres in order, so ties
+ * go to the last centre; best starts at FLT_MAX and the cell at 0. */
+void orc_voronoi(const float* X, int64_t n, const float* C, int64_t m, int64_t d, int64_t* cell, float* dist)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float best = 3.40282346638528859812e+38F;
+        int64_t bi = 0;
+        for (int64_t c = 0; c < m; ++c) {
+            float v = orc_l2seq(C + c * d, X + i * d, d);
+            if (v <= best) {
+                best = v;
+                bi = c;
+            }
+        }
+        cell[i] = bi;
+        dist[i] = best;
+    }
+}
+
 /* ------------------------------------------------------------------ simplices */
 
 int64_t orc_binom(int64_t n, int64_t k)

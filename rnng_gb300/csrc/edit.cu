@@ -1,0 +1,493 @@
+// Epsilon graph under RNNG's edit distance (drivers/systolic.cpp:271-299: unit-cost
+// Levenshtein distance, returned as a float; edge iff distance <= radius).
+//
+// All arithmetic is integer, so the result is exact by construction:
+//   1. strings are sorted by length and cut into tiles of 128;
+//   2. a tile pair is considered only when some of its strings differ in length by at
+//      most K = floor(radius) (the length difference is a lower bound of the distance);
+//   3. every pair of a considered tile pair passes two sound filters: |len a - len b|
+//      <= K, and the L1 distance of hashed 3-gram profiles <= 2 * 3 * K (one edit
+//      changes at most q = 3 q-grams out and q in; merging q-grams into 64 hash bins and
+//      saturating counts only lowers L1, so no pair within K is rejected);
+//   4. every surviving pair gets a banded dynamic program over the diagonals |i-j| <= K
+//      with cell values capped at K+1.  Cells outside the band exceed K anyway, so the
+//      band gives the exact distance whenever it is <= K (Ukkonen's cut-off).
+// Distances above K are never reported, so the cap never shows in the output.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+#include "eps_l2.cuh"
+#include "kernels_misc.cuh"
+
+namespace rnng {
+
+constexpr int kET = 128;      // strings per tile
+constexpr int kBins = 64;     // hashed 3-gram profile bins (one byte each)
+constexpr int kQ = 3;
+
+__global__ void k_edit_lengths(const int64_t* __restrict__ off, int64_t n, uint32_t* __restrict__ len,
+                               int32_t* __restrict__ idx)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        len[i] = (uint32_t)(off[i + 1] - off[i]);
+        idx[i] = (int32_t)i;
+    }
+}
+
+__device__ __forceinline__ int qgram_bin(uint32_t a, uint32_t b, uint32_t c)
+{
+    return (int)(((a * 0x9E3779B1u) ^ (b * 0x85EBCA77u) ^ (c * 0xC2B2AE3Du)) >> 26);
+}
+
+// Profile of sorted string p (64 saturating byte counts); padding rows get zeros.
+__global__ void __launch_bounds__(128) k_edit_profiles(const uint8_t* __restrict__ atoms,
+                                                       const int64_t* __restrict__ off,
+                                                       const int32_t* __restrict__ perm, int64_t n, int64_t n_pad,
+                                                       uint32_t* __restrict__ prof)
+{
+    __shared__ uint8_t h[128][kBins];
+    for (int64_t base = (int64_t)blockIdx.x * 128; base < n_pad; base += (int64_t)gridDim.x * 128) {
+        const int64_t p = base + threadIdx.x;
+        for (int b = 0; b < kBins; ++b) h[threadIdx.x][b] = 0;
+        if (p < n) {
+            const int64_t o = off[perm[p]], m = off[perm[p] + 1] - o;
+            for (int64_t i = 0; i + kQ <= m; ++i) {
+                const int b = qgram_bin(atoms[o + i], atoms[o + i + 1], atoms[o + i + 2]);
+                if (h[threadIdx.x][b] < 255) h[threadIdx.x][b]++;
+            }
+        }
+        const uint32_t* hw = reinterpret_cast<const uint32_t*>(h[threadIdx.x]);
+        for (int k = 0; k < kBins / 4; ++k) prof[p * (kBins / 4) + k] = hw[k];
+        __syncthreads();
+    }
+}
+
+// Tile t's string lengths: [min, max] over its real strings (sorted ascending).
+__global__ void k_edit_tile_len(const uint32_t* __restrict__ slen, int64_t n, int64_t T, uint32_t* __restrict__ lo,
+                                uint32_t* __restrict__ hi)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+        lo[t] = slen[t * kET];
+        hi[t] = slen[min(n, (t + 1) * kET) - 1];
+    }
+}
+
+// Number of partner tiles j >= i whose shortest string is within K of tile i's longest.
+__global__ void k_edit_ranges(const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi, int64_t T, int K,
+                              int32_t* __restrict__ cnt)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t lim = (uint64_t)hi[i] + (uint64_t)K;
+        int64_t a = i, b = T;  // first j with lo[j] > lim
+        while (a < b) {
+            const int64_t m = (a + b) / 2;
+            if ((uint64_t)lo[m] <= lim) a = m + 1;
+            else b = m;
+        }
+        cnt[i] = (int32_t)(a - i);
+    }
+}
+
+__global__ void k_edit_emit_pairs(const int32_t* __restrict__ cnt, const int32_t* __restrict__ off, int64_t T,
+                                  int2* __restrict__ pairs)
+{
+    for (int64_t i = blockIdx.x; i < T; i += gridDim.x)
+        for (int k = threadIdx.x; k < cnt[i]; k += blockDim.x) pairs[off[i] + k] = make_int2((int)i, (int)(i + k));
+}
+
+// Filter: length and profile L1 tests for all pairs of each tile pair; survivors are
+// appended as (sorted index a, sorted index b), a < b.
+__global__ void __launch_bounds__(256) k_edit_filter(const uint32_t* __restrict__ prof,
+                                                     const uint32_t* __restrict__ slen, int64_t n,
+                                                     const int2* __restrict__ pairs, int64_t npairs, int K,
+                                                     uint2* __restrict__ cand, unsigned long long* __restrict__ ccount,
+                                                     unsigned long long cap)
+{
+    __shared__ uint32_t pa[kET][kBins / 4 + 1], pb[kET][kBins / 4 + 1];
+    __shared__ uint32_t la[kET], lb[kET];
+    __shared__ int s_warp[8];
+    __shared__ unsigned long long s_base;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15, lane = tid & 31, warp = tid >> 5;
+    const uint32_t thr = (uint32_t)(2 * kQ * K);
+    for (int64_t w = blockIdx.x; w < npairs; w += gridDim.x) {
+        const int2 tp = pairs[w];
+        const int64_t i0 = (int64_t)tp.x * kET, j0 = (int64_t)tp.y * kET;
+        __syncthreads();
+        for (int idx = tid; idx < kET * (kBins / 4); idx += 256) {
+            const int r = idx / (kBins / 4), k = idx % (kBins / 4);
+            pa[r][k] = prof[(i0 + r) * (kBins / 4) + k];
+            pb[r][k] = prof[(j0 + r) * (kBins / 4) + k];
+        }
+        for (int r = tid; r < kET; r += 256) {
+            la[r] = i0 + r < n ? slen[i0 + r] : 0xffffffffu;
+            lb[r] = j0 + r < n ? slen[j0 + r] : 0xffffffffu;
+        }
+        __syncthreads();
+        uint64_t mask = 0;  // 8 x 8 block of this thread
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int ra = ty * 8 + r;
+            const uint32_t l1 = la[ra];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int cb = tx * 8 + c;
+                const uint32_t l2 = lb[cb];
+                const uint32_t dl = l1 > l2 ? l1 - l2 : l2 - l1;
+                bool ok = (l1 != 0xffffffffu) && (l2 != 0xffffffffu) && dl <= (uint32_t)K &&
+                          (tp.x != tp.y || ra < cb);
+                if (ok) {
+                    uint32_t s = 0;
+#pragma unroll
+                    for (int k = 0; k < kBins / 4; ++k) s = __vsadu4(pa[ra][k], pb[cb][k]) + s;
+                    ok = s <= thr;
+                }
+                mask |= (uint64_t)(ok ? 1u : 0u) << (r * 8 + c);
+            }
+        }
+        const int nhit = __popcll(mask);
+        int incl = nhit;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (tid == 0) {
+            int a = 0;
+            for (int k = 0; k < 8; ++k) { const int t = s_warp[k]; s_warp[k] = a; a += t; }
+            s_base = a ? atomicAdd(ccount, (unsigned long long)a) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long pos = s_base + (unsigned long long)(s_warp[warp] + incl - nhit);
+        while (mask) {
+            const int b = __ffsll((long long)mask) - 1;
+            mask &= mask - 1;
+            if (pos < cap) cand[pos] = make_uint2((uint32_t)(i0 + ty * 8 + b / 8), (uint32_t)(j0 + tx * 8 + b % 8));
+            ++pos;
+        }
+    }
+}
+
+// Banded edit distance, band half-width B >= K, values capped at K + 1.
+template <int B>
+__device__ int banded_edit(const uint8_t* __restrict__ s, int m, const uint8_t* __restrict__ t, int n, int K)
+{
+    constexpr int W = 2 * B + 1;
+    const int INF = K + 1;
+    int prev[W], cur[W];
+    // row 0: D[0][j] = j for j = k - B in [0, n]
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const int j = k - B;
+        prev[k] = (j >= 0 && j <= n) ? min(j, INF) : INF;
+    }
+    // window of t: tw[k] = t[i + k - B - 1] for the current row i (0 outside)
+    int tw[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const int j = 1 + k - B - 1;  // row i = 1
+        tw[k] = (j >= 0 && j < n) ? (int)t[j] : -1;
+    }
+    for (int i = 1; i <= m; ++i) {
+        const int si = (int)s[i - 1];
+        int rowmin = INF;
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const int j = i + k - B;
+            int v;
+            if (j < 0 || j > n) {
+                v = INF;
+            } else if (j == 0) {
+                v = min(i, INF);
+            } else {
+                const int diag = prev[k] + (si == tw[k] ? 0 : 1);
+                const int up = (k + 1 < W ? prev[k + 1] : INF) + 1;
+                const int left = (k > 0 ? cur[k - 1] : INF) + 1;
+                v = min(min(diag, up), min(left, INF));
+            }
+            cur[k] = v;
+            rowmin = min(rowmin, v);
+        }
+        if (rowmin > K) return INF;
+#pragma unroll
+        for (int k = 0; k < W; ++k) prev[k] = cur[k];
+        // slide the t window by one for row i + 1
+#pragma unroll
+        for (int k = 0; k + 1 < W; ++k) tw[k] = tw[k + 1];
+        {
+            const int j = i + 1 + (W - 1) - B - 1;
+            tw[W - 1] = (j >= 0 && j < n) ? (int)t[j] : -1;
+        }
+    }
+    const int k = n - m + B;
+    return (k >= 0 && k < W) ? prev[k] : INF;
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_edit_verify(const uint8_t* __restrict__ atoms,
+                                                     const int64_t* __restrict__ off,
+                                                     const int32_t* __restrict__ perm, const uint2* __restrict__ cand,
+                                                     const unsigned long long* __restrict__ ncand_ptr,
+                                                     unsigned long long ccap, int K, uint32_t* __restrict__ eu,
+                                                     uint32_t* __restrict__ ev, float* __restrict__ ew,
+                                                     unsigned long long* __restrict__ ecount, unsigned long long cap)
+{
+    __shared__ int s_warp[8];
+    __shared__ unsigned long long s_base;
+    const unsigned long long nc = min(*ncand_ptr, ccap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long round = (unsigned long long)blockIdx.x * blockDim.x; round < nc; round += stride) {
+        const unsigned long long e = round + threadIdx.x;
+        bool hit = false;
+        int dist = 0;
+        uint2 c = make_uint2(0, 0);
+        if (e < nc) {
+            c = cand[e];
+            const int64_t oa = off[perm[c.x]], ob = off[perm[c.y]];
+            const int ma = (int)(off[perm[c.x] + 1] - oa), mb = (int)(off[perm[c.y] + 1] - ob);
+            // the reference computes EditDistance(indexed point, query); the distance is symmetric
+            dist = banded_edit<B>(atoms + oa, ma, atoms + ob, mb, K);
+            hit = dist <= K;
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) s_warp[warp] = __popc(ball);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int a = 0;
+            for (int k = 0; k < 8; ++k) { const int t = s_warp[k]; s_warp[k] = a; a += t; }
+            s_base = a ? atomicAdd(ecount, (unsigned long long)a) : 0ull;
+        }
+        __syncthreads();
+        if (hit) {
+            const unsigned long long pos = s_base + s_warp[warp] + __popc(ball & ((1u << lane) - 1u));
+            if (pos < cap) {
+                eu[pos] = c.x;
+                ev[pos] = c.y;
+                ew[pos] = (float)dist;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_edit_finalize(const uint32_t* __restrict__ si, const uint32_t* __restrict__ sj,
+                                const float* __restrict__ sw, int64_t m, const int32_t* __restrict__ perm,
+                                const int64_t* __restrict__ ids, int64_t* __restrict__ u, int64_t* __restrict__ v,
+                                float* __restrict__ w)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t a = perm[si[e]], b = perm[sj[e]];
+        const int64_t ia = ids ? ids[a] : (int64_t)a, ib = ids ? ids[b] : (int64_t)b;
+        u[e] = ia < ib ? ia : ib;
+        v[e] = ia < ib ? ib : ia;
+        w[e] = sw[e];
+    }
+}
+
+}  // namespace rnng
+
+using namespace rnng;
+
+extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int64_t* offsets, const int64_t* ids,
+                                   int64_t n, float radius, unsigned flags, rnng_edges* out)
+{
+    if (!c) return RNNG_ERR_INVALID;
+    try {
+        RNNG_CUDA(cudaSetDevice(c->device));
+        RNNG_REQUIRE(out != nullptr, RNNG_ERR_INVALID, "out is null");
+        std::memset(out, 0, sizeof(*out));
+        RNNG_REQUIRE(n >= 0 && (n == 0 || (atoms && offsets)), RNNG_ERR_INVALID, "bad strings");
+        RNNG_REQUIRE(n < (int64_t(1) << 31) - kET, RNNG_ERR_INVALID, "too many strings");
+        RNNG_REQUIRE(radius == radius, RNNG_ERR_INVALID, "radius is NaN");
+        c->stats = rnng_stats{};
+        c->launches = 0;
+        cudaStream_t s = c->stream;
+        const int K = radius < 0.f ? -1 : (int)std::min(std::floor((double)radius), 1e9);
+        RNNG_REQUIRE(K <= 32, RNNG_ERR_UNSUPPORTED, "edit-distance radius above 32 is not supported");
+        // inputs
+        int64_t natoms = 0;
+        const int64_t* doff = offsets;
+        const uint8_t* datoms = atoms;
+        const int64_t* dids = ids;
+        if (!(flags & RNNG_INPUT_DEVICE)) {
+            natoms = n > 0 ? offsets[n] : 0;
+            c->ids_in.reserve(sizeof(int64_t) * (size_t)(n + 1));
+            c->x_in.reserve(std::max<size_t>((size_t)natoms, 1));
+            RNNG_CUDA(cudaMemcpyAsync(c->ids_in.ptr, offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
+            if (natoms) RNNG_CUDA(cudaMemcpyAsync(c->x_in.ptr, atoms, (size_t)natoms, cudaMemcpyHostToDevice, s));
+            doff = c->ids_in.as<int64_t>();
+            datoms = c->x_in.as<uint8_t>();
+            if (ids) {
+                c->aux7.reserve(sizeof(int64_t) * (size_t)std::max<int64_t>(n, 1));
+                RNNG_CUDA(cudaMemcpyAsync(c->aux7.ptr, ids, sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+                dids = c->aux7.as<int64_t>();
+            }
+        }
+        int64_t m = 0;
+        c->out_u.reserve(8);
+        c->out_v.reserve(8);
+        c->out_w.reserve(8);
+        if (n >= 2 && K >= 0) {
+            const int64_t T = ceil_div(n, kET), n_pad = T * kET;
+            RNNG_REQUIRE(T < 65536, RNNG_ERR_UNSUPPORTED, "more than 8M strings per call");
+            const unsigned g = (unsigned)std::min<int64_t>(ceil_div(n, 256), (int64_t)c->num_sms * 8);
+            // 1. sort by length
+            c->keys.reserve(sizeof(uint32_t) * 2 * n_pad);
+            c->perm.reserve(sizeof(int32_t) * 2 * n_pad);
+            uint32_t* len = c->keys.as<uint32_t>();
+            uint32_t* slen = len + n_pad;
+            int32_t* idx = c->perm.as<int32_t>();
+            int32_t* perm = idx + n_pad;
+            k_edit_lengths<<<g, 256, 0, s>>>(doff, n, len, idx);
+            ++c->launches;
+            size_t tmp = 0;
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, len, slen, idx, perm, (int)n, 0, 32, s));
+            c->cub_tmp.reserve(tmp);
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, len, slen, idx, perm, (int)n, 0, 32, s));
+            c->launches += cub_sort_kernels(n, 32);
+            // 2. profiles and tile length ranges
+            c->x_sorted.reserve(sizeof(uint32_t) * (size_t)n_pad * (kBins / 4));
+            uint32_t* prof = c->x_sorted.as<uint32_t>();
+            k_edit_profiles<<<(unsigned)std::min<int64_t>(T, (int64_t)c->num_sms * 8), 128, 0, s>>>(
+                datoms, doff, perm, n, n_pad, prof);
+            ++c->launches;
+            c->aux2.reserve(sizeof(uint32_t) * 2 * (size_t)T + sizeof(int32_t) * 2 * ((size_t)T + 1));
+            uint32_t* tlo = c->aux2.as<uint32_t>();
+            uint32_t* thi = tlo + T;
+            int32_t* tcnt = (int32_t*)(thi + T);
+            int32_t* toff = tcnt + T + 1;
+            const unsigned gt = (unsigned)std::min<int64_t>(ceil_div(T, 256), (int64_t)c->num_sms * 8);
+            k_edit_tile_len<<<gt, 256, 0, s>>>(slen, n, T, tlo, thi);
+            k_edit_ranges<<<gt, 256, 0, s>>>(tlo, thi, T, K, tcnt);
+            c->launches += 2;
+            exclusive_scan_i32(c, tcnt, toff, T + 1);
+            int32_t npairs = 0;
+            RNNG_CUDA(cudaMemcpyAsync(&npairs, toff + T, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            c->pair_list.reserve(sizeof(int2) * (size_t)std::max(npairs, 1));
+            k_edit_emit_pairs<<<(unsigned)std::min<int64_t>(T, (int64_t)c->num_sms * 8), 128, 0, s>>>(
+                tcnt, toff, T, c->pair_list.as<int2>());
+            ++c->launches;
+            c->stats.tile_pairs = npairs;
+            c->stats.tile_pairs_all = T * (T + 1) / 2;
+            c->stats.pairs_evaluated = (int64_t)npairs * kET * kET;
+            // 3. filter
+            c->counters.reserve(sizeof(unsigned long long) * 8);
+            unsigned long long* ccount = c->counters.as<unsigned long long>() + 2;
+            unsigned long long* ecount = c->counters.as<unsigned long long>() + 3;
+            unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
+            unsigned long long got = 0;
+            const unsigned gf = (unsigned)std::max<int64_t>(1, std::min<int64_t>(npairs, (int64_t)c->num_sms * 8));
+            for (int attempt = 0;; ++attempt) {
+                c->cand.reserve(sizeof(uint2) * ccap);
+                RNNG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), s));
+                if (npairs > 0) {
+                    k_edit_filter<<<gf, 256, 0, s>>>(prof, slen, n, c->pair_list.as<int2>(), npairs, K,
+                                                     c->cand.as<uint2>(), ccount, ccap);
+                    ++c->launches;
+                }
+                RNNG_CUDA(cudaMemcpyAsync(&got, ccount, sizeof(got), cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaStreamSynchronize(s));
+                if (got <= ccap) break;
+                RNNG_REQUIRE(attempt < 2, RNNG_ERR_OVERFLOW, "candidate buffer overflow after regrowth");
+                ccap = got + got / 8 + 1024;
+            }
+            c->cand_cap_hint = std::max<unsigned long long>(c->cand_cap_hint, got + got / 8);
+            c->stats.candidates = (int64_t)got;
+            // 4. exact banded verification
+            unsigned long long ecap = std::max<unsigned long long>(1u << 20, c->edge_cap_hint);
+            unsigned long long egot = 0;
+            const unsigned gv = (unsigned)std::max<unsigned long long>(
+                1, std::min<unsigned long long>((got + 255) / 256, (unsigned long long)c->num_sms * 16));
+            for (int attempt = 0;; ++attempt) {
+                c->edges_u.reserve(sizeof(uint32_t) * ecap);
+                c->edges_v.reserve(sizeof(uint32_t) * ecap);
+                c->edges_w.reserve(sizeof(float) * ecap);
+                RNNG_CUDA(cudaMemsetAsync(ecount, 0, sizeof(unsigned long long), s));
+                if (got > 0) {
+                    auto* eu = c->edges_u.as<uint32_t>();
+                    auto* ev = c->edges_v.as<uint32_t>();
+                    auto* ew = c->edges_w.as<float>();
+                    if (K <= 4)
+                        k_edit_verify<4><<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap, K,
+                                                            eu, ev, ew, ecount, ecap);
+                    else if (K <= 8)
+                        k_edit_verify<8><<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap, K,
+                                                            eu, ev, ew, ecount, ecap);
+                    else if (K <= 16)
+                        k_edit_verify<16><<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap,
+                                                             K, eu, ev, ew, ecount, ecap);
+                    else
+                        k_edit_verify<32><<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap,
+                                                             K, eu, ev, ew, ecount, ecap);
+                    ++c->launches;
+                    RNNG_CUDA(cudaGetLastError());
+                }
+                RNNG_CUDA(cudaMemcpyAsync(&egot, ecount, sizeof(egot), cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaStreamSynchronize(s));
+                if (egot <= ecap) break;
+                RNNG_REQUIRE(attempt < 2, RNNG_ERR_OVERFLOW, "edge buffer overflow after regrowth");
+                ecap = egot + egot / 8 + 1024;
+            }
+            c->edge_cap_hint = std::max<unsigned long long>(c->edge_cap_hint, egot + egot / 8);
+            m = (int64_t)egot;
+            c->out_u.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
+            c->out_v.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
+            c->out_w.reserve(sizeof(float) * std::max<int64_t>(m, 1));
+            if (m) {
+                k_edit_finalize<<<(unsigned)std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8), 256, 0,
+                                  s>>>(c->edges_u.as<uint32_t>(), c->edges_v.as<uint32_t>(), c->edges_w.as<float>(),
+                                       m, perm, dids, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(),
+                                       c->out_w.as<float>());
+                ++c->launches;
+                if (flags & RNNG_SORT_OUTPUT)
+                    sort_edges_uv(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m);
+            }
+        }
+        // deliver
+        out->count = m;
+        out->staged = 1;
+        if (flags & RNNG_OUTPUT_DEVICE) {
+            out->on_device = 1;
+            out->u = c->out_u.as<int64_t>();
+            out->v = c->out_v.as<int64_t>();
+            out->w = c->out_w.as<float>();
+        } else {
+            const size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1);
+            const size_t bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
+            DevBuf& slot = c->host_stage;
+            if (2 * bi + bf > slot.bytes) {
+                if (slot.ptr) cudaFreeHost(slot.ptr);
+                slot.ptr = nullptr;
+                slot.bytes = 0;
+                RNNG_CUDA(cudaMallocHost(&slot.ptr, 2 * bi + bf + 256));
+                slot.bytes = 2 * bi + bf + 256;
+            }
+            char* h = (char*)slot.ptr;
+            out->u = (int64_t*)h;
+            out->v = (int64_t*)(h + bi);
+            out->w = (float*)(h + 2 * bi);
+            if (m) {
+                RNNG_CUDA(cudaMemcpyAsync(out->u, c->out_u.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaMemcpyAsync(out->v, c->out_v.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaMemcpyAsync(out->w, c->out_w.ptr, sizeof(float) * m, cudaMemcpyDeviceToHost, s));
+            }
+        }
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        c->stats.edges = m;
+        c->stats.kernel_launches = c->launches;
+        c->last_error.clear();
+        return RNNG_OK;
+    } catch (const Error& e) {
+        c->last_error = e.msg;
+        return e.code;
+    } catch (...) {
+        c->last_error = "unknown error";
+        return RNNG_ERR_INVALID;
+    }
+}

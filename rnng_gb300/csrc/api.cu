@@ -136,6 +136,32 @@ int64_t tiles_with_retry(rnng_ctx* c, Layout& L, int mode, EdgeOut& E)
 
 }  // namespace
 
+namespace rnng {
+
+// The L2 epsilon-graph pipeline on device-resident points (n >= 2, radius >= 0):
+// partition, covers, pruning, tiles.  Edges stay in sorted-index space in E; the
+// context events 2..5 (and 8..10 in BF16 mode) mark the stages.
+int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, int mode, Layout& L, EdgeOut& E)
+{
+    cudaStream_t s = c->stream;
+    L = build_layout(c, dX, n, d, radius);
+    RNNG_CUDA(cudaEventRecord(c->ev[2], s));
+    build_covers(c, L);
+    RNNG_CUDA(cudaEventRecord(c->ev[3], s));
+    prune_covers(c, L);
+    RNNG_CUDA(cudaEventRecord(c->ev[4], s));
+    if (mode == RNNG_MODE_BF16_RECHECK) {
+        schedule_pairs(c, L, (int)std::max<unsigned long long>(
+                                 1, std::min<unsigned long long>(L.tile_pairs, (unsigned long long)c->num_sms)));
+        prepare_bf16(c, L);
+    }
+    const int64_t m = tiles_with_retry(c, L, mode, E);
+    RNNG_CUDA(cudaEventRecord(c->ev[5], s));
+    return m;
+}
+
+}  // namespace rnng
+
 extern "C" {
 
 int rnng_ctx_create(int device, rnng_ctx** out)
@@ -241,26 +267,15 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
             // no pair can be an edge (a negative radius admits no distance)
             RNNG_CUDA(cudaEventRecord(c->ev[2], s));
             c->out_u.reserve(8);
-        c->out_v.reserve(8);
-        c->out_w.reserve(8);
-        deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), 0, flags, out);
+            c->out_v.reserve(8);
+            c->out_w.reserve(8);
+            deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), 0, flags, out);
             RNNG_CUDA(cudaStreamSynchronize(s));
             return;
         }
-        Layout L = build_layout(c, dX, n, (int)d, radius);
-        RNNG_CUDA(cudaEventRecord(c->ev[2], s));
-        build_covers(c, L);
-        RNNG_CUDA(cudaEventRecord(c->ev[3], s));
-        prune_covers(c, L);
-        RNNG_CUDA(cudaEventRecord(c->ev[4], s));
-        if (mode == RNNG_MODE_BF16_RECHECK) {
-            schedule_pairs(c, L, (int)std::max<unsigned long long>(
-                                     1, std::min<unsigned long long>(L.tile_pairs, (unsigned long long)c->num_sms)));
-            prepare_bf16(c, L);
-        }
+        Layout L;
         EdgeOut E;
-        int64_t m = tiles_with_retry(c, L, mode, E);
-        RNNG_CUDA(cudaEventRecord(c->ev[5], s));
+        const int64_t m = eps_core(c, dX, n, (int)d, radius, mode, L, E);
         c->out_u.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
         c->out_v.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
         c->out_w.reserve(sizeof(float) * std::max<int64_t>(m, 1));

@@ -47,6 +47,9 @@ void sort_pairs_u64(rnng_ctx* c, uint64_t* keys_in, uint64_t* keys_out, int32_t*
 // out[0..count-1] = exclusive prefix sum of in[0..count-2] (in[count-1] is zeroed first).
 void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t count);
 
+// The whole L2 pipeline on device points (api.cu); edges in sorted-index space in E.
+int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, int mode, Layout& L, EdgeOut& E);
+
 // BF16 tensor-core Gram tiles with FP32 recheck (gram_bf16.cu).
 void prepare_bf16(rnng_ctx* c, Layout& L);
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E);

@@ -1,0 +1,102 @@
+// Drop-in edge list with the interface of RNNG's include/graph.h: construction sorts the
+// edges, redistribute_edges gives every rank both orientations of its vertices' edges
+// (sorted, duplicates removed), write_file prints a MatrixMarket-like text file.
+#ifndef RNNG_DROPIN_GRAPH_H_
+#define RNNG_DROPIN_GRAPH_H_
+
+#include "utils.h"
+
+class Graph
+{
+  public:
+    using Edge = std::tuple<Index, Index, Real>;
+    using EdgeVector = std::vector<Edge>;
+
+    Graph(const EdgeVector& edges, Index num_vertices) : edges(edges), num_vertices(num_vertices)
+    {
+        std::sort(this->edges.begin(), this->edges.end());
+    }
+
+    // "% n n m" then "u v w" with w printed "%.6f" (RNNG include/graph.hpp:1-17).
+    void write_file(const char* fname) const
+    {
+        FILE* f = std::fopen(fname, "w");
+        assert((f != nullptr));
+        std::fprintf(f, "%% %lld %lld %lld\n", (long long)num_vertices, (long long)num_vertices,
+                     (long long)edges.size());
+        for (const auto& [u, v, w] : edges) std::fprintf(f, "%lld %lld %.6f\n", (long long)u, (long long)v, w);
+        std::fclose(f);
+    }
+
+    // Collective version: each rank's text at its offset of one file, the header on
+    // rank 0, weights with six significant digits (RNNG include/graph.hpp:20-56).
+    void write_file(const char* fname, MPI_Comm comm) const
+    {
+        int rank = 0;
+        MPI_Comm_rank(comm, &rank);
+        Index total = (Index)edges.size();
+        MPI_Allreduce(MPI_IN_PLACE, &total, 1, MPI_INDEX, MPI_SUM, comm);
+        std::ostringstream out;
+        if (rank == 0) out << "% " << num_vertices << " " << num_vertices << " " << total << "\n";
+        out << std::setprecision(6);
+        for (const auto& [u, v, w] : edges) out << u << " " << v << " " << w << "\n";
+        const std::string text = out.str();
+        assert((text.size() <= (size_t)std::numeric_limits<int>::max()));
+        MPI_Offset mine = (MPI_Offset)text.size(), at = 0, size = 0;
+        MPI_Exscan(&mine, &at, 1, MPI_OFFSET, MPI_SUM, comm);
+        if (rank == 0) at = 0;
+        MPI_File fh;
+        MPI_File_open(comm, fname, MPI_MODE_CREATE | MPI_MODE_WRONLY, MPI_INFO_NULL, &fh);
+        MPI_File_get_size(fh, &size);
+        int truncate = size > 0;
+        MPI_Bcast(&truncate, 1, MPI_INT, 0, comm);
+        if (truncate) MPI_File_set_size(fh, 0);
+        MPI_File_write_at_all(fh, at, text.data(), (int)text.size(), MPI_CHAR, MPI_STATUS_IGNORE);
+        MPI_File_close(&fh);
+    }
+
+    // Both orientations of every edge go to the owners of their first vertex (blocks of
+    // num_vertices / ranks), then sort and unique (RNNG include/graph.hpp:59-116).  The
+    // edges recorded by the drop-in queries already hold every self-loop; a whole-graph
+    // caller can get this list directly on the GPU with rnng_graph_finalize.
+    void redistribute_edges(MPI_Comm comm)
+    {
+        int rank = 0, nranks = 1;
+        MPI_Comm_rank(comm, &rank);
+        MPI_Comm_size(comm, &nranks);
+        const Index chunk = std::max<Index>(1, num_vertices / nranks);
+        auto owner = [&](Index x) { return (int)std::min<Index>(x / chunk, nranks - 1); };
+        MPI_Datatype edge_t;
+        MPI_Type_contiguous(sizeof(Edge), MPI_CHAR, &edge_t);
+        MPI_Type_commit(&edge_t);
+        std::vector<int> scount(nranks, 0), sdisp(nranks), rcount(nranks), rdisp(nranks);
+        for (const auto& [u, v, w] : edges) {
+            scount[owner(u)]++;
+            scount[owner(v)]++;
+        }
+        std::exclusive_scan(scount.begin(), scount.end(), sdisp.begin(), 0);
+        EdgeVector send((size_t)sdisp.back() + scount.back()), recv;
+        std::vector<int> fill = sdisp;
+        for (const auto& [u, v, w] : edges) {
+            send[fill[owner(u)]++] = Edge(u, v, w);
+            send[fill[owner(v)]++] = Edge(v, u, w);
+        }
+        MPI_Alltoall(scount.data(), 1, MPI_INT, rcount.data(), 1, MPI_INT, comm);
+        std::exclusive_scan(rcount.begin(), rcount.end(), rdisp.begin(), 0);
+        recv.resize((size_t)rdisp.back() + rcount.back());
+        MPI_Alltoallv(send.data(), scount.data(), sdisp.data(), edge_t, recv.data(), rcount.data(), rdisp.data(),
+                      edge_t, comm);
+        MPI_Type_free(&edge_t);
+        std::sort(recv.begin(), recv.end());
+        recv.erase(std::unique(recv.begin(), recv.end()), recv.end());
+        edges.swap(recv);
+    }
+
+    Index num_edges() const { return (Index)edges.size(); }
+
+  private:
+    EdgeVector edges;
+    Index num_vertices;
+};
+
+#endif  // RNNG_DROPIN_GRAPH_H_

@@ -67,13 +67,16 @@ typedef struct rnng_edges {
     int staged;    /* 1: arrays owned by the context (not freed by rnng_edges_free) */
 } rnng_edges;
 
-/* A filtration: simplex ids (RNNG's Simplex encoding, include/simplex.hpp:5-19) and values. */
+/* A filtration: simplex ids (RNNG's Simplex encoding, include/simplex.hpp:5-19) and values.
+ * flag (rnng_rips_edges with vertex flags, else NULL): 1 when one of the simplex's
+ * vertices is flagged, RNNG's `interior` of a WeightedSimplex (include/point.hpp:1160-1168). */
 typedef struct rnng_simplices {
     int64_t count;
     int64_t* id;
     float* value;
     int on_device;
     int staged;
+    uint8_t* flag;
 } rnng_simplices;
 
 /* Counters and stage times of the last call on a context (milliseconds). */
@@ -129,6 +132,14 @@ int rnng_radius_query_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int6
 int rnng_voronoi_l2(rnng_ctx* ctx, const float* X, int64_t n, const float* C, int64_t m, int64_t d,
                     unsigned flags, int64_t* cell, float* dist);
 
+/* Nearest landmark per string under edit distance, same tie rule and output as
+ * rnng_voronoi_l2: VoronoiDiagram<char>::VoronoiDiagram (include/point.hpp:537-559) with
+ * the drivers' EditDistance<char> (drivers/landmark.cpp:354-383).  Strings and centres
+ * in RNNG's CSR layout (atoms, offsets[count + 1]); centres up to 4096 characters. */
+int rnng_voronoi_edit(rnng_ctx* ctx, const uint8_t* atoms, const int64_t* offsets, int64_t n,
+                      const uint8_t* centre_atoms, const int64_t* centre_offsets, int64_t m, unsigned flags,
+                      int64_t* cell, float* dist);
+
 /* Epsilon graph, edit distance -------------------------------------------------------------
  * Strings in RNNG's CSR layout (include/point.h:77-79): atoms[offsets[i] .. offsets[i+1]).
  * Replaces the drivers' edit-distance path (drivers/landmark.cpp:61-62 with
@@ -139,11 +150,23 @@ int rnng_eps_graph_edit(rnng_ctx* ctx, const uint8_t* atoms, const int64_t* offs
 /* Vietoris-Rips filtration ----------------------------------------------------------------
  * Replaces VoronoiComplex::build_filtration per cell + merge_and_write_filtration
  * (include/point.hpp:1136-1267, include/simplex.hpp:130-196, drivers/rips.cpp:174-245):
- * all vertices (value 0), edges (value = L2) and, for maxdim >= 2, triangles (value =
- * max edge), ids per include/simplex.hpp:5-19 over the point ids, sorted by (value, id).
- * maxdim is 0, 1 or 2. */
+ * all vertices (value 0), edges (value = L2) and every clique of up to maxdim + 1
+ * vertices (value = its largest edge, RNNG's max over facets), ids per
+ * include/simplex.hpp:5-19 over the point ids, sorted by (value, id).  maxdim is 0..15
+ * (the id keeps the dimension in 4 bits); RNNG's rips driver defaults to 3. */
 int rnng_rips_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
                  int maxdim, int mode, unsigned flags, rnng_simplices* out);
+
+/* The same filtration for a graph the caller already has: VoronoiComplex::build_filtration
+ * after its neighbour graph is built (include/point.hpp:1146-1230), for any metric (the
+ * drop-in headers use it for edit-distance complexes and for cells cut from a cached
+ * whole-set graph).  Vertices are rows 0..n-1 with ids (NULL = the rows) and optional
+ * vertex_flags (nonzero = flagged; NULL = none, out->flag stays NULL); u[e], v[e] are
+ * rows (either order) and w[e] >= 0 the edge's value; each unordered pair at most once.
+ * RNNG_ERR_INVALID for rows out of range, self-loops, repeated pairs, negative or NaN
+ * values; -0 is taken as +0. */
+int rnng_rips_edges(rnng_ctx* ctx, int64_t n, const int64_t* ids, const uint8_t* vertex_flags, const int64_t* u,
+                    const int64_t* v, const float* w, int64_t m, int maxdim, unsigned flags, rnng_simplices* out);
 
 /* Graph finalisation: Graph(edges) + redistribute_edges at one rank
  * (include/graph.h:14, include/graph.hpp:59-116): from unordered edges, the list of

@@ -55,6 +55,11 @@ def lib() -> ctypes.CDLL:
         L.orc_rips.argtypes = [ctypes.c_int64, _i64p, _i64p, _f32p, ctypes.c_int64, ctypes.c_int,
                                ctypes.POINTER(_i64p), ctypes.POINTER(_f32p)]
         L.orc_voronoi.argtypes = [_f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int64, _i64p, _f32p]
+        L.orc_voronoi_edit.argtypes = [ctypes.c_void_p, _i64p, ctypes.c_int64, ctypes.c_void_p, _i64p,
+                                       ctypes.c_int64, _i64p, _f32p]
+        L.orc_dist_matrix_l2.argtypes = [_f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int64, _f32p]
+        L.orc_dist_matrix_edit.argtypes = [ctypes.c_void_p, _i64p, ctypes.c_int64, ctypes.c_void_p, _i64p,
+                                           ctypes.c_int64, _f32p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -142,6 +147,147 @@ def voronoi(X: np.ndarray, C: np.ndarray):
     return cell, dist
 
 
+def voronoi_edit(atoms: np.ndarray, offsets: np.ndarray, catoms: np.ndarray, coffsets: np.ndarray):
+    """Nearest centre per string under the reference edit distance (last of equal wins)."""
+    atoms = np.ascontiguousarray(atoms, np.uint8)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    catoms = np.ascontiguousarray(catoms, np.uint8)
+    coffsets = np.ascontiguousarray(coffsets, np.int64)
+    n, m = offsets.size - 1, coffsets.size - 1
+    cell = np.zeros(n, np.int64)
+    dist = np.zeros(n, np.float32)
+    lib().orc_voronoi_edit(atoms.ctypes.data_as(ctypes.c_void_p), offsets.ctypes.data_as(_i64p), n,
+                           catoms.ctypes.data_as(ctypes.c_void_p), coffsets.ctypes.data_as(_i64p), m,
+                           cell.ctypes.data_as(_i64p), dist.ctypes.data_as(_f32p))
+    return cell, dist
+
+
+class _Points:
+    """Dense float rows (L2) or CSR strings (edit distance), the oracle's view of a
+    PointContainer."""
+
+    def __init__(self, metric, data):
+        self.metric = metric
+        if metric == "l2":
+            self.x = np.ascontiguousarray(data, np.float32)
+            self.n = self.x.shape[0]
+        else:
+            atoms, offsets = data
+            self.atoms = np.ascontiguousarray(atoms, np.uint8)
+            self.offsets = np.ascontiguousarray(offsets, np.int64)
+            self.n = self.offsets.size - 1
+
+    def rows(self, idx):
+        idx = np.asarray(idx, np.int64)
+        if self.metric == "l2":
+            return _Points("l2", self.x[idx])
+        parts = [self.atoms[self.offsets[i]:self.offsets[i + 1]] for i in idx]
+        offs = np.zeros(idx.size + 1, np.int64)
+        offs[1:] = np.cumsum([p.size for p in parts]) if parts else []
+        atoms = np.concatenate(parts) if parts else np.zeros(0, np.uint8)
+        return _Points("edit", (atoms, offs))
+
+    def dist_matrix(self, centres: "_Points") -> np.ndarray:
+        """out[i, c] = distance(centre c, point i), the reference's float arithmetic."""
+        out = np.zeros((self.n, centres.n), np.float32)
+        if self.n == 0 or centres.n == 0:
+            return out
+        if self.metric == "l2":
+            lib().orc_dist_matrix_l2(self.x.ctypes.data_as(_f32p), self.n, centres.x.ctypes.data_as(_f32p), centres.n,
+                                     self.x.shape[1], out.ctypes.data_as(_f32p))
+        else:
+            lib().orc_dist_matrix_edit(self.atoms.ctypes.data_as(ctypes.c_void_p), self.offsets.ctypes.data_as(_i64p),
+                                       self.n, centres.atoms.ctypes.data_as(ctypes.c_void_p),
+                                       centres.offsets.ctypes.data_as(_i64p), centres.n, out.ctypes.data_as(_f32p))
+        return out
+
+    def eps_graph(self, radius):
+        if self.metric == "l2":
+            return eps_graph_l2(self.x, radius)
+        return eps_graph_edit(self.atoms, self.offsets, radius)
+
+
+def landmark_cells(metric: str, data, landmarks, radius, rips: bool) -> dict:
+    """The Voronoi cells of RNNG's landmark and rips drivers at one rank, restated:
+
+    VoronoiDiagram (include/point.hpp:537-559): nearest landmark, last of equal wins.
+    coalesce_cells (include/point.hpp:562-758): cells in landmark order, points in row
+    order (id = row), the landmark's own point swapped into slot 0; a cell that got no
+    point keeps id 0 (its id is only set from received points).
+    add_ghost_points_systolic[_rips] (include/point.hpp:762-1124): every point q of cell A
+    (in cell order) with its distance dq to A's landmark is tested against the k-th
+    non-empty cell's slot-0 point s_k: when distance(s_k, q) <= dq + 2r, the cell at index
+    k (cells[k], which is the k-th non-empty cell only when no cell is empty) gets q as
+    a ghost if it is not empty, does not hold q, and has a point within r of q.  The
+    rips version marks a point interior when it became nobody's ghost.
+
+    Returns the flattened cell arrays of the harness's `cells` dump."""
+    pts = _Points(metric, data)
+    radius = np.float32(radius)
+    landmarks = np.asarray(landmarks, np.int64)
+    cents = pts.rows(landmarks)
+    m = landmarks.size
+    dmat = pts.dist_matrix(cents)  # (n, m)
+    cell = np.zeros(pts.n, np.int64)
+    dist = np.full(pts.n, np.float32(np.finfo(np.float32).max), np.float32)
+    for c in range(m):  # `dist <= best`, centres in order
+        upd = dmat[:, c] <= dist
+        dist[upd] = dmat[upd, c]
+        cell[upd] = c
+    cells = []
+    for c in range(m):
+        rows = list(np.nonzero(cell == c)[0])
+        dd = [dist[r] for r in rows]
+        if rows:
+            slot = next((k for k, r in enumerate(rows) if r == landmarks[c]), 0)
+            rows[0], rows[slot] = rows[slot], rows[0]
+            dd[0], dd[slot] = dd[slot], dd[0]
+        cells.append({"id": c if rows else 0, "rows": rows, "dist": dd, "ghosts": [], "interior": [False] * len(rows)})
+    # ghosts
+    nonempty = [k for k, cl in enumerate(cells) if cl["rows"]]
+    slot0 = pts.rows([cells[k]["rows"][0] for k in nonempty])
+    qrows = [r for cl in cells for r in cl["rows"]]
+    qdist = np.array([d for cl in cells for d in cl["dist"]], np.float32)
+    to_slot0 = pts.rows(qrows).dist_matrix(slot0) if qrows else np.zeros((0, 0), np.float32)
+    u, v, _ = pts.eps_graph(radius)
+    nbrs = [set() for _ in range(pts.n)]
+    for a, b in zip(u.tolist(), v.tolist()):
+        nbrs[a].add(b)
+        nbrs[b].add(a)
+    own = [set(cl["rows"]) for cl in cells]       # the points each cell's cover tree holds
+    members = [set(cl["rows"]) for cl in cells]   # treeids_set: own points and tested ids
+    shared = np.zeros(len(qrows), np.int64)
+    two_r = np.float32(2) * radius
+    for qi, q in enumerate(qrows):
+        bound = np.float32(qdist[qi] + two_r)
+        for k in range(len(nonempty)):
+            if not (to_slot0[qi, k] <= bound):
+                continue
+            target = cells[k]
+            if not target["rows"] or q in members[k]:
+                continue
+            if nbrs[q] & own[k]:
+                target["ghosts"].append(q)
+                shared[qi] += 1
+            members[k].add(q)  # the tested id joins the cell's id set (treeids_set)
+    if rips:
+        qi = 0
+        for cl in cells:
+            for j in range(len(cl["rows"])):
+                cl["interior"][j] = shared[qi] == 0
+                qi += 1
+    res = {
+        "cell_id": np.array([cl["id"] for cl in cells], np.int64),
+        "npts": np.array([len(cl["rows"]) for cl in cells], np.int64),
+        "ids": np.array([r for cl in cells for r in cl["rows"]], np.int64),
+        "dist": np.array([d for cl in cells for d in cl["dist"]], np.float32),
+        "interior": np.array([b for cl in cells for b in cl["interior"]], np.uint8),
+        "nghost": np.array([len(cl["ghosts"]) for cl in cells], np.int64),
+        "ghosts": np.array([g for cl in cells for g in cl["ghosts"]], np.int64),
+    }
+    return res
+
+
 def binom(n: int, k: int) -> int:
     return int(lib().orc_binom(n, k))
 
@@ -152,7 +298,8 @@ def simplex_id(verts) -> int:
 
 
 def rips(n: int, u: np.ndarray, v: np.ndarray, w: np.ndarray, maxdim: int = 2):
-    """Filtration (ids, values) sorted by (value, id) from an epsilon graph with u < v."""
+    """Filtration (ids, values) sorted by (value, id) from an epsilon graph with u < v
+    over vertices 0..n-1, cliques up to maxdim + 1 vertices."""
     u = np.ascontiguousarray(u, np.int64)
     v = np.ascontiguousarray(v, np.int64)
     w = np.ascontiguousarray(w, np.float32)
@@ -183,6 +330,41 @@ def read_simplex_dump(path: str):
         ids = np.frombuffer(f.read(8 * n), np.int64)
         vals = np.frombuffer(f.read(4 * n), np.float32)
     return ids, vals
+
+
+def read_cells_dump(path: str) -> dict:
+    """Cells written by the harness's `cells` mode, flattened: landmarks, cell_id, npts,
+    ids, dist, interior, nghost, ghosts (per-cell runs concatenated in cell order)."""
+    with open(path, "rb") as f:
+        buf = f.read()
+    pos = 0
+
+    def take(dtype, count):
+        nonlocal pos
+        a = np.frombuffer(buf, dtype, count, pos)
+        pos += a.nbytes
+        return a
+
+    nland = int(take(np.int64, 1)[0])
+    landmarks = take(np.int64, nland).copy()
+    ncell = int(take(np.int64, 1)[0])
+    out = {k: [] for k in ("cell_id", "npts", "ids", "dist", "interior", "nghost", "ghosts")}
+    for _ in range(ncell):
+        out["cell_id"].append(int(take(np.int64, 1)[0]))
+        npts = int(take(np.int64, 1)[0])
+        out["npts"].append(npts)
+        out["ids"].append(take(np.int64, npts))
+        out["dist"].append(take(np.float32, npts))
+        out["interior"].append(take(np.uint8, npts))
+        ng = int(take(np.int64, 1)[0])
+        out["nghost"].append(ng)
+        out["ghosts"].append(take(np.int64, ng))
+    assert pos == len(buf)
+    res = {"landmarks": landmarks, "cell_id": np.array(out["cell_id"], np.int64),
+           "npts": np.array(out["npts"], np.int64), "nghost": np.array(out["nghost"], np.int64)}
+    for k, dt in (("ids", np.int64), ("dist", np.float32), ("interior", np.uint8), ("ghosts", np.int64)):
+        res[k] = np.concatenate(out[k]).astype(dt) if out[k] else np.zeros(0, dt)
+    return res
 
 
 def reference_graph_semantics(u, v, w):

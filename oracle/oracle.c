@@ -18,6 +18,7 @@
  *   orc_binom            include/utils.hpp:116-144 (Binom::operator(): int64 falling
  *                        product divided by k!)
  *   orc_simplex_id       include/simplex.hpp:5-19 (Simplex(verts): sum C(v_i, i+1) | dim<<60)
+ *   orc_voronoi[_edit]   include/point.hpp:537-559 (VoronoiDiagram: `dist <= best`, last wins)
  *   orc_rips             include/point.hpp:1136-1232 (build_filtration: vertex value 0,
  *                        edge value = distance, higher simplex = max over facets) and
  *                        include/simplex.hpp:130-196 (merge: sort by (value, id), unique id)
@@ -254,6 +255,24 @@ void orc_voronoi(const float* X, int64_t n, const float* C, int64_t m, int64_t d
     }
 }
 
+/* All n x m reference distances distance(C[c], X[i]) into out[i * m + c]. */
+void orc_dist_matrix_l2(const float* X, int64_t n, const float* C, int64_t m, int64_t d, float* out)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t c = 0; c < m; ++c) out[i * m + c] = orc_l2seq(C + c * d, X + i * d, d);
+}
+
+void orc_dist_matrix_edit(const uint8_t* atoms, const int64_t* offsets, int64_t n, const uint8_t* catoms,
+                          const int64_t* coffsets, int64_t m, float* out)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t c = 0; c < m; ++c)
+            out[i * m + c] = orc_edit(catoms + coffsets[c], coffsets[c + 1] - coffsets[c], atoms + offsets[i],
+                                      offsets[i + 1] - offsets[i]);
+}
+
 /* ------------------------------------------------------------------ simplices */
 
 int64_t orc_binom(int64_t n, int64_t k)
@@ -289,10 +308,62 @@ static int cmp_simplex(const void* a, const void* b)
     return 0;
 }
 
-/* Vietoris-Rips filtration up to dimension 2 from an epsilon graph given as
- * unordered edges (u < v) with their reference distances.  Emits every vertex
- * (value 0), every edge (value w) and every triangle a<b<c (value max of its three
- * edge weights), sorted by (value, id) with ids unique.  maxdim may be 0, 1 or 2. */
+typedef struct {
+    const int64_t* deg; /* CSR of higher-numbered neighbours: deg[v] .. deg[v+1] */
+    const int64_t* nbr;
+    const float* nw;
+    int maxdim;
+    simplex_rec* out;
+    int64_t cnt, cap;
+} rips_walk;
+
+static void rips_emit(rips_walk* r, const int64_t* verts, int64_t k, float value)
+{
+    if (r->cnt == r->cap) {
+        r->cap = r->cap * 2 + 1024;
+        r->out = (simplex_rec*)realloc(r->out, sizeof(simplex_rec) * (size_t)r->cap);
+    }
+    memcpy(&r->out[r->cnt].vbits, &value, 4);
+    r->out[r->cnt].id = orc_simplex_id(verts, k);
+    r->cnt++;
+}
+
+/* verts[0..k) is a clique (ascending) of value `value`; cand[0..nc) are the vertices
+ * above verts[k-1] adjacent to all of it, cw[i] the largest edge from the clique to
+ * cand[i].  Emits every clique that extends verts by candidates, up to maxdim + 1
+ * vertices, each once (vertices are added in increasing order). */
+static void rips_grow(rips_walk* r, int64_t* verts, int64_t k, float value, const int64_t* cand, const float* cw,
+                      int64_t nc)
+{
+    if (k == (int64_t)r->maxdim + 1) return;
+    int64_t* nc2 = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nc ? nc : 1));
+    float* cw2 = (float*)malloc(sizeof(float) * (size_t)(nc ? nc : 1));
+    for (int64_t i = 0; i < nc; ++i) {
+        const int64_t y = cand[i];
+        const float vy = cw[i] > value ? cw[i] : value;
+        verts[k] = y;
+        rips_emit(r, verts, k + 1, vy);
+        /* candidates after y that are neighbours of y: merge with N+(y) */
+        int64_t m2 = 0, p = r->deg[y];
+        for (int64_t j = i + 1; j < nc; ++j) {
+            while (p < r->deg[y + 1] && r->nbr[p] < cand[j]) ++p;
+            if (p < r->deg[y + 1] && r->nbr[p] == cand[j]) {
+                nc2[m2] = cand[j];
+                cw2[m2] = cw[j] > r->nw[p] ? cw[j] : r->nw[p];
+                ++m2;
+            }
+        }
+        rips_grow(r, verts, k + 1, vy, nc2, cw2, m2);
+    }
+    free(nc2);
+    free(cw2);
+}
+
+/* Vietoris-Rips filtration up to dimension maxdim (0..15) from an epsilon graph given
+ * as unordered edges (u < v) with their reference distances.  Emits every vertex
+ * (value 0) and every clique of 2 .. maxdim+1 vertices with the largest of its edge
+ * weights as value (for edges the weight itself; above, RNNG's max over facets equals
+ * the max over all edges), sorted by (value, id) with ids unique. */
 int64_t orc_rips(int64_t n, const int64_t* eu, const int64_t* ev, const float* ew, int64_t m, int maxdim,
                  int64_t** ids, float** values)
 {
@@ -325,51 +396,17 @@ int64_t orc_rips(int64_t n, const int64_t* eu, const int64_t* ev, const float* e
         }
     }
 
-    int64_t cap = n + (maxdim >= 1 ? m : 0) + 1024, cnt = 0;
-    simplex_rec* out = (simplex_rec*)malloc(sizeof(simplex_rec) * (size_t)cap);
-    for (int64_t i = 0; i < n; ++i) {
-        out[cnt].vbits = 0;
-        out[cnt].id = orc_simplex_id(&i, 1);
-        cnt++;
+    rips_walk r = {deg, nbr, nw, maxdim, NULL, 0, 0};
+    r.cap = n + (maxdim >= 1 ? m : 0) + 1024;
+    r.out = (simplex_rec*)malloc(sizeof(simplex_rec) * (size_t)r.cap);
+    int64_t verts[16];
+    for (int64_t a = 0; a < n; ++a) {
+        verts[0] = a;
+        rips_emit(&r, verts, 1, 0.f);
+        rips_grow(&r, verts, 1, 0.f, nbr + deg[a], nw + deg[a], deg[a + 1] - deg[a]);
     }
-    if (maxdim >= 1) {
-        for (int64_t a = 0; a < n; ++a)
-            for (int64_t p = deg[a]; p < deg[a + 1]; ++p) {
-                int64_t vv[2] = {a, nbr[p]};
-                memcpy(&out[cnt].vbits, &nw[p], 4);
-                out[cnt].id = orc_simplex_id(vv, 2);
-                cnt++;
-            }
-    }
-    if (maxdim >= 2) {
-        for (int64_t a = 0; a < n; ++a) {
-            for (int64_t p = deg[a]; p < deg[a + 1]; ++p) {
-                int64_t b = nbr[p];
-                float wab = nw[p];
-                /* intersect N+(a) beyond b with N+(b) */
-                int64_t x = p + 1, y = deg[b];
-                while (x < deg[a + 1] && y < deg[b + 1]) {
-                    if (nbr[x] < nbr[y]) ++x;
-                    else if (nbr[x] > nbr[y]) ++y;
-                    else {
-                        float wv = wab;
-                        if (nw[x] > wv) wv = nw[x];
-                        if (nw[y] > wv) wv = nw[y];
-                        if (cnt == cap) {
-                            cap *= 2;
-                            out = (simplex_rec*)realloc(out, sizeof(simplex_rec) * (size_t)cap);
-                        }
-                        int64_t vv[3] = {a, b, nbr[x]};
-                        memcpy(&out[cnt].vbits, &wv, 4);
-                        out[cnt].id = orc_simplex_id(vv, 3);
-                        cnt++;
-                        ++x;
-                        ++y;
-                    }
-                }
-            }
-        }
-    }
+    simplex_rec* out = r.out;
+    const int64_t cnt = r.cnt;
     qsort(out, (size_t)cnt, sizeof(simplex_rec), cmp_simplex);
     int64_t k = 0;
     for (int64_t i = 0; i < cnt; ++i)
@@ -386,4 +423,27 @@ int64_t orc_rips(int64_t n, const int64_t* eu, const int64_t* ev, const float* e
     free(nw);
     free(fill);
     return k;
+}
+
+/* Nearest centre per string as VoronoiDiagram<char> with the drivers' EditDistance
+ * (include/point.hpp:537-559, drivers/landmark.cpp:354-383): `dist <= best` over the
+ * centres in order (ties to the last), best from FLT_MAX, cell from 0. */
+void orc_voronoi_edit(const uint8_t* atoms, const int64_t* offsets, int64_t n, const uint8_t* catoms,
+                      const int64_t* coffsets, int64_t m, int64_t* cell, float* dist)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+        float best = 3.40282346638528859812e+38F;
+        int64_t bi = 0;
+        for (int64_t c = 0; c < m; ++c) {
+            float v = orc_edit(catoms + coffsets[c], coffsets[c + 1] - coffsets[c], atoms + offsets[i],
+                               offsets[i + 1] - offsets[i]);
+            if (v <= best) {
+                best = v;
+                bi = c;
+            }
+        }
+        cell[i] = bi;
+        dist[i] = best;
+    }
 }

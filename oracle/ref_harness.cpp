@@ -12,11 +12,18 @@
 //   systolic <in.fvecs> <radius> <out>          drivers/systolic.cpp:96-147
 //   landmark <l2|edit> <in> <radius> <m> <seed> <out>
 //                                                drivers/landmark.cpp:111-210
-//   rips <in.fvecs> <radius> <maxdim> <m> <seed> <out>
+//   rips <l2|edit> <in> <radius> <maxdim> <m> <seed> <out>
 //                                                drivers/rips.cpp:106-180
+//   cells <l2|edit> <in> <radius> <m> <seed> <rips 0|1> <out>
+//                                                drivers/landmark.cpp:111-175 and
+//                                                drivers/rips.cpp:106-162: the Voronoi
+//                                                cells after coalescing and ghosts
 // Edge output: int64 count, then count int64 u, count int64 v, count float32 w
 // (u = query id, v = indexed id, as the drivers' functors record them).
 // Simplex output: int64 count, count int64 ids, count float32 values.
+// Cell output: int64 m, m int64 landmark rows, int64 cell count, then per cell: int64 cell id, int64 np, np int64 point
+// ids, np float32 distances to the centre, np uint8 interior flags, int64 ng, ng int64
+// ghost ids.
 #include <mpi.h>
 
 #include "graph.h"
@@ -139,25 +146,33 @@ static int run_landmark(const char* in, Real radius, Index m, int seed, const ch
     return 0;
 }
 
+template <class Atom>
+static Index read_points(PointContainer<Atom>& points, const char* in, MPI_Comm comm)
+{
+    if constexpr (std::is_same_v<Atom, char>) return points.read_seqs(in, comm);
+    else return points.read_fvecs(in, comm);
+}
+
+template <class Atom, class Distance>
 static int run_rips(const char* in, Real radius, Index maxdim, Index m, int seed, const char* out)
 {
     MPI_Comm comm = MPI_COMM_WORLD;
-    PointContainer<float> points;
-    Index n = points.read_fvecs(in, comm);
+    Distance distance;
+    PointContainer<Atom> points;
+    const Index n = read_points(points, in, comm);
     IndexVector landmarks;
     selection_sample(n, m, landmarks, seed);
-    PointContainer<float> mycenters, centers;
+    PointContainer<Atom> mycenters, centers;
     mycenters.indexed_gather(points, landmarks);
     centers.allgather(mycenters, comm);
-    HarnessL2<float> distance;
-    VoronoiDiagram<float> diagram(points, centers, distance);
-    std::vector<VoronoiCell<float>> cells;
+    VoronoiDiagram<Atom> diagram(points, centers, distance);
+    std::vector<VoronoiCell<Atom>> cells;
     diagram.coalesce_cells(cells, comm);
     diagram.add_ghost_points_systolic_rips(cells, distance, radius, 1.5, 10, comm);
     std::vector<int64_t> ids;
     std::vector<float> values;
-    for (const VoronoiCell<float>& cell : cells) {
-        VoronoiComplex<float> vc(cell, radius, maxdim);
+    for (const VoronoiCell<Atom>& cell : cells) {
+        VoronoiComplex<Atom> vc(cell, radius, maxdim);
         vc.build_filtration(distance, n, 1.5, 10);
         for (auto it = vc.begin(); it != vc.end(); ++it) {
             ids.push_back(it->getid());
@@ -174,6 +189,49 @@ static int run_rips(const char* in, Real radius, Index maxdim, Index m, int seed
     return 0;
 }
 
+template <class Atom, class Distance>
+static int run_cells(const char* in, Real radius, Index m, int seed, bool rips, const char* out)
+{
+    MPI_Comm comm = MPI_COMM_WORLD;
+    Distance distance;
+    PointContainer<Atom> points;
+    const Index n = read_points(points, in, comm);
+    assert((m <= n));
+    IndexVector landmarks;
+    selection_sample(n, m, landmarks, seed);
+    PointContainer<Atom> mycenters, centers;
+    mycenters.indexed_gather(points, landmarks);
+    centers.allgather(mycenters, comm);
+    VoronoiDiagram<Atom> diagram(points, centers, distance);
+    std::vector<VoronoiCell<Atom>> cells;
+    diagram.coalesce_cells(cells, comm);
+    if (rips) diagram.add_ghost_points_systolic_rips(cells, distance, radius, 1.5, 10, comm);
+    else diagram.add_ghost_points_systolic(cells, distance, radius, 1.5, 10, comm);
+    FILE* f = std::fopen(out, "wb");
+    if (!f) { std::perror(out); return 2; }
+    auto put = [&](int64_t x) { std::fwrite(&x, sizeof(x), 1, f); };
+    put((int64_t)landmarks.size());
+    for (Index l : landmarks) put(l);
+    put((int64_t)cells.size());
+    for (const VoronoiCell<Atom>& cell : cells) {
+        put(cell.id());
+        put(cell.num_points());
+        for (Index i = 0; i < cell.num_points(); ++i) put(cell[i].id());
+        for (Index i = 0; i < cell.num_points(); ++i) {
+            const float d = cell.dist_to_center(i);
+            std::fwrite(&d, sizeof(d), 1, f);
+        }
+        for (Index i = 0; i < cell.num_points(); ++i) {
+            const uint8_t b = cell.interiors()[i] ? 1 : 0;
+            std::fwrite(&b, 1, 1, f);
+        }
+        put(cell.num_ghosts());
+        for (Index i = 0; i < cell.num_ghosts(); ++i) put(cell.ghost(i).id());
+    }
+    std::fclose(f);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     MPI_Init(&argc, &argv);
@@ -186,15 +244,26 @@ int main(int argc, char** argv)
         int seed = std::atoi(argv[6]);
         if (!std::strcmp(argv[2], "edit")) rc = run_landmark<char, HarnessEdit<char>>(argv[3], r, m, seed, argv[7]);
         else rc = run_landmark<float, HarnessL2<float>>(argv[3], r, m, seed, argv[7]);
-    } else if (argc == 8 && !std::strcmp(argv[1], "rips")) {
-        rc = run_rips(argv[2], (Real)std::atof(argv[3]), std::atoll(argv[4]), std::atoll(argv[5]), std::atoi(argv[6]),
-                      argv[7]);
+    } else if (argc == 9 && !std::strcmp(argv[1], "rips")) {
+        const Real r = (Real)std::atof(argv[4]);
+        const Index maxdim = std::atoll(argv[5]), m = std::atoll(argv[6]);
+        const int seed = std::atoi(argv[7]);
+        if (!std::strcmp(argv[2], "edit")) rc = run_rips<char, HarnessEdit<char>>(argv[3], r, maxdim, m, seed, argv[8]);
+        else rc = run_rips<float, HarnessL2<float>>(argv[3], r, maxdim, m, seed, argv[8]);
+    } else if (argc == 9 && !std::strcmp(argv[1], "cells")) {
+        const Real r = (Real)std::atof(argv[4]);
+        const Index m = std::atoll(argv[5]);
+        const int seed = std::atoi(argv[6]);
+        const bool rips = std::atoi(argv[7]) != 0;
+        if (!std::strcmp(argv[2], "edit")) rc = run_cells<char, HarnessEdit<char>>(argv[3], r, m, seed, rips, argv[8]);
+        else rc = run_cells<float, HarnessL2<float>>(argv[3], r, m, seed, rips, argv[8]);
     } else {
         std::fprintf(stderr,
                      "usage: %s systolic <in.fvecs> <radius> <out>\n"
                      "       %s landmark <l2|edit> <in> <radius> <m> <seed> <out>\n"
-                     "       %s rips <in.fvecs> <radius> <maxdim> <m> <seed> <out>\n",
-                     argv[0], argv[0], argv[0]);
+                     "       %s rips <l2|edit> <in> <radius> <maxdim> <m> <seed> <out>\n"
+                     "       %s cells <l2|edit> <in> <radius> <m> <seed> <rips 0|1> <out>\n",
+                     argv[0], argv[0], argv[0], argv[0]);
     }
     MPI_Finalize();
     return rc;

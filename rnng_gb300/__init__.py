@@ -37,6 +37,7 @@ EXPORTS = [
     "rnng_ctx_create", "rnng_ctx_destroy", "rnng_last_error", "rnng_get_stats", "rnng_ctx_stream", "rnng_ctx_trim",
     "rnng_eps_graph_l2", "rnng_radius_query_l2", "rnng_voronoi_l2", "rnng_eps_graph_edit", "rnng_rips_l2",
     "rnng_graph_finalize", "rnng_edges_free", "rnng_simplices_free", "rnng_eps_graph_l2_static",
+    "rnng_voronoi_edit", "rnng_rips_edges",
 ]
 
 
@@ -53,7 +54,7 @@ class Edges(ctypes.Structure):
 
 class Simplices(ctypes.Structure):
     _fields_ = [("count", ctypes.c_int64), ("id", ctypes.c_void_p), ("value", ctypes.c_void_p),
-                ("on_device", ctypes.c_int), ("staged", ctypes.c_int)]
+                ("on_device", ctypes.c_int), ("staged", ctypes.c_int), ("flag", ctypes.c_void_p)]
 
 
 class Stats(ctypes.Structure):
@@ -96,6 +97,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rnng_graph_finalize.argtypes = [vp, ctypes.POINTER(Edges), i64, u32, ctypes.POINTER(Edges)]
     L.rnng_edges_free.argtypes = [ctypes.POINTER(Edges)]
     L.rnng_simplices_free.argtypes = [ctypes.POINTER(Simplices)]
+    L.rnng_voronoi_edit.argtypes = [vp, vp, vp, i64, vp, vp, i64, u32, vp, vp]
+    L.rnng_rips_edges.argtypes = [vp, i64, vp, vp, vp, vp, vp, i64, ip, u32, ctypes.POINTER(Simplices)]
     L.rnng_eps_graph_l2_static.argtypes = [vp, vp, i64, i64, f32, vp, vp, vp, i64, ctypes.POINTER(i64), vp]
     _lib = L
     return L
@@ -107,6 +110,21 @@ def _ptr(a) -> int | None:
     if isinstance(a, np.ndarray):
         return a.ctypes.data
     return int(a.data_ptr())  # torch tensor (device or pinned host)
+
+
+def _csr(seqs):
+    """(atoms uint8, offsets int64) from a list of bytes or an (atoms, offsets) pair."""
+    if isinstance(seqs, tuple):
+        atoms, offsets = seqs
+    else:
+        lens = np.fromiter((len(s) for s in seqs), dtype=np.int64, count=len(seqs))
+        offsets = np.zeros(len(seqs) + 1, np.int64)
+        np.cumsum(lens, out=offsets[1:])
+        atoms = np.frombuffer(b"".join(seqs), np.uint8) if seqs else np.zeros(0, np.uint8)
+    atoms = np.ascontiguousarray(atoms, np.uint8)
+    if atoms.size == 0:
+        atoms = np.zeros(1, np.uint8)
+    return atoms, np.ascontiguousarray(offsets, np.int64)
 
 
 def _host_copy(ptr: int, n: int, dtype) -> np.ndarray:
@@ -220,23 +238,25 @@ class Context:
     # ------------------------------------------------------------------ edit distance
     def eps_graph_edit(self, seqs, radius, ids=None, sort: bool = True):
         """seqs: list of bytes, or (atoms uint8, offsets int64) in CSR form."""
-        if isinstance(seqs, tuple):
-            atoms, offsets = seqs
-        else:
-            lens = np.fromiter((len(s) for s in seqs), dtype=np.int64, count=len(seqs))
-            offsets = np.zeros(len(seqs) + 1, np.int64)
-            np.cumsum(lens, out=offsets[1:])
-            atoms = np.frombuffer(b"".join(seqs), np.uint8) if seqs else np.zeros(0, np.uint8)
-        atoms = np.ascontiguousarray(atoms, np.uint8)
-        if atoms.size == 0:
-            atoms = np.zeros(1, np.uint8)
-        offsets = np.ascontiguousarray(offsets, np.int64)
+        atoms, offsets = _csr(seqs)
         ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
         e = Edges()
         rc = self.lib.rnng_eps_graph_edit(self.h, _ptr(atoms), _ptr(offsets), _ptr(ids), offsets.size - 1,
                                           ctypes.c_float(radius), SORT_OUTPUT if sort else 0, ctypes.byref(e))
         self._check(rc, self.h)
         return self._edges_out(e)
+
+    def voronoi_edit(self, seqs, centres):
+        """Nearest centre per string (edit distance, last of equal wins): (cell, dist)."""
+        atoms, offsets = _csr(seqs)
+        catoms, coffsets = _csr(centres)
+        n = offsets.size - 1
+        cell = np.zeros(max(n, 1), np.int64)
+        dist = np.zeros(max(n, 1), np.float32)
+        rc = self.lib.rnng_voronoi_edit(self.h, _ptr(atoms), _ptr(offsets), n, _ptr(catoms), _ptr(coffsets),
+                                        coffsets.size - 1, 0, _ptr(cell), _ptr(dist))
+        self._check(rc, self.h)
+        return cell[:n], dist[:n]
 
     # ------------------------------------------------------------------ Rips
     def rips_l2(self, X, radius, maxdim: int = 2, mode: str = "bf16", ids=None):
@@ -247,6 +267,24 @@ class Context:
                                    MODES[mode], SORT_OUTPUT, ctypes.byref(s))
         self._check(rc, self.h)
         return _host_copy(s.id, s.count, np.int64), _host_copy(s.value, s.count, np.float32)
+
+    def rips_edges(self, n: int, u, v, w, maxdim: int = 2, ids=None, vertex_flags=None):
+        """Filtration of a given graph over rows 0..n-1 (edges u, v with values w):
+        (ids, values), plus per-simplex flags when vertex_flags is given."""
+        u = np.ascontiguousarray(u, np.int64)
+        v = np.ascontiguousarray(v, np.int64)
+        w = np.ascontiguousarray(w, np.float32)
+        ids = None if ids is None else np.ascontiguousarray(ids, np.int64)
+        vf = None if vertex_flags is None else np.ascontiguousarray(vertex_flags, np.uint8)
+        s = Simplices()
+        rc = self.lib.rnng_rips_edges(self.h, n, _ptr(ids), _ptr(vf), _ptr(u) if u.size else None,
+                                      _ptr(v) if v.size else None, _ptr(w) if w.size else None, u.size, maxdim, 0,
+                                      ctypes.byref(s))
+        self._check(rc, self.h)
+        out = (_host_copy(s.id, s.count, np.int64), _host_copy(s.value, s.count, np.float32))
+        if vf is not None:
+            out += (_host_copy(s.flag, s.count, np.uint8),)
+        return out
 
     def graph_finalize(self, u, v, w, num_vertices: int):
         """Both orientations plus self-loops, sorted by (u, v) (Graph::redistribute_edges)."""

@@ -16,45 +16,11 @@ using namespace rnng;
 
 namespace {
 
-template <class F>
-int guarded(rnng_ctx* ctx, F&& body)
-{
-    if (!ctx) return RNNG_ERR_INVALID;
-    try {
-        RNNG_CUDA(cudaSetDevice(ctx->device));
-        body();
-        ctx->last_error.clear();
-        return RNNG_OK;
-    } catch (const Error& e) {
-        ctx->last_error = e.msg;
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        ctx->last_error = "host allocation failed";
-        return RNNG_ERR_NOMEM;
-    } catch (...) {
-        ctx->last_error = "unknown error";
-        return RNNG_ERR_INVALID;
-    }
-}
-
 float elapsed(rnng_ctx* c, int a, int b)
 {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev[a], c->ev[b]) != cudaSuccess) return 0.f;
     return ms;
-}
-
-void* stage(rnng_ctx* c, DevBuf& slot, size_t bytes)
-{
-    // DevBuf is reused here for a pinned host block: ptr from cudaMallocHost.
-    if (bytes <= slot.bytes) return slot.ptr;
-    if (slot.ptr) cudaFreeHost(slot.ptr);
-    slot.ptr = nullptr;
-    slot.bytes = 0;
-    size_t grow = bytes + bytes / 4 + 256;
-    RNNG_CUDA(cudaMallocHost(&slot.ptr, grow));
-    slot.bytes = grow;
-    return slot.ptr;
 }
 
 const float* upload_f32(rnng_ctx* c, DevBuf& buf, const float* X, int64_t count, unsigned flags)
@@ -72,35 +38,6 @@ const int64_t* upload_i64(rnng_ctx* c, DevBuf& buf, const int64_t* v, int64_t co
     buf.reserve(sizeof(int64_t) * (size_t)std::max<int64_t>(count, 1));
     if (count) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, v, sizeof(int64_t) * count, cudaMemcpyHostToDevice, c->stream));
     return buf.as<int64_t>();
-}
-
-// Hands the device edge arrays (u, v, w of length m) to the caller, either as new
-// device allocations or copied into the pinned staging area.
-void deliver_edges(rnng_ctx* c, const int64_t* du, const int64_t* dv, const float* dw, int64_t m, unsigned flags,
-                   rnng_edges* out)
-{
-    std::memset(out, 0, sizeof(*out));
-    out->count = m;
-    size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1), bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
-    if (flags & RNNG_OUTPUT_DEVICE) {
-        // the context's own result buffers, valid until the next call
-        out->on_device = 1;
-        out->staged = 1;
-        out->u = const_cast<int64_t*>(du);
-        out->v = const_cast<int64_t*>(dv);
-        out->w = const_cast<float*>(dw);
-    } else {
-        out->staged = 1;
-        char* h = (char*)stage(c, c->host_stage, 2 * bi + bf);
-        out->u = (int64_t*)h;
-        out->v = (int64_t*)(h + bi);
-        out->w = (float*)(h + 2 * bi);
-        if (m) {
-            RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
-            RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
-            RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream));
-        }
-    }
 }
 
 // Runs the tile stage, growing the edge buffer and re-running when it overflowed.
@@ -232,7 +169,8 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->keys_alt, &c->perm_alt, &c->cell, &c->dist, &c->pivots, &c->tile_lo, &c->tile_hi,
                           &c->super_lo, &c->super_hi, &c->pair_list, &c->super_list, &c->counters, &c->edges_u,
                           &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
-                          &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched};
+                          &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
+                          &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -79,7 +80,8 @@ struct rnng_ctx {
     // named scratch buffers
     rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
-        out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched;
+        out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched, clq0, clq1,
+        hi_id, hi_val, hi_flag, sflag, vflag;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;
     int64_t last_candidates = 0;
@@ -99,6 +101,29 @@ struct rnng_ctx {
 };
 
 namespace rnng {
+
+// Runs an entry point's body on the context's device and turns exceptions into a
+// status code, keeping the message for rnng_last_error().
+template <class F>
+int guarded(rnng_ctx* ctx, F&& body)
+{
+    if (!ctx) return RNNG_ERR_INVALID;
+    try {
+        RNNG_CUDA(cudaSetDevice(ctx->device));
+        body();
+        ctx->last_error.clear();
+        return RNNG_OK;
+    } catch (const Error& e) {
+        ctx->last_error = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        ctx->last_error = "host allocation failed";
+        return RNNG_ERR_NOMEM;
+    } catch (...) {
+        ctx->last_error = "unknown error";
+        return RNNG_ERR_INVALID;
+    }
+}
 
 inline void ensure_events(rnng_ctx* c)
 {

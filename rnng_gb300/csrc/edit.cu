@@ -16,6 +16,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <cfloat>
 #include <cstring>
 
 #include "common.cuh"
@@ -289,6 +290,113 @@ __global__ void k_edit_finalize(const uint32_t* __restrict__ si, const uint32_t*
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Nearest centre under edit distance (rnng_voronoi_edit).
+//
+// Full (unbanded) unit-cost Levenshtein distance by Myers' bit-vector algorithm (G. Myers,
+// "A fast bit-vector algorithm for approximate string matching based on dynamic
+// programming", J. ACM 46(3), 1999), in its multi-word block form, computing the whole-
+// string distance as H. Hyyro describes it: the DP column of the centre (the pattern,
+// one bit per character) is kept as vertical +1/-1 delta vectors Pv/Mv, the first row
+// D[0][j] = j feeds a +1 horizontal delta into the first word at every text column, and
+// the distance D[m][n] is m plus the horizontal deltas that leave pattern row m.  Rows
+// only depend on the rows above them, so the padding bits of the last word never reach
+// row m.  The result is the integer distance, converted to float like the reference's.
+
+constexpr int kVE = 128;     // points (texts) per block
+constexpr int kVEMaxW = 64;  // 64-bit words per centre: centres up to 4096 characters
+
+template <int WT>  // WT > 0: at most WT words in registers; WT == 0: any W <= kVEMaxW
+__device__ __forceinline__ int myers_distance(const unsigned long long* __restrict__ peq, int W, int lp,
+                                              const uint8_t* __restrict__ t, int64_t lt)
+{
+    constexpr int kCap = WT > 0 ? WT : kVEMaxW;
+    unsigned long long Pv[kCap], Mv[kCap];
+#pragma unroll
+    for (int w = 0; w < kCap; ++w) {
+        Pv[w] = ~0ull;
+        Mv[w] = 0ull;
+    }
+    const unsigned long long last_bit = 1ull << ((lp - 1) & 63);
+    const int nw = WT > 0 ? WT : W;  // with WT > 0 the words past W see Eq = 0 and are ignored
+    int score = lp;
+    for (int64_t j = 0; j < lt; ++j) {
+        const unsigned long long* eq = peq + (int)t[j] * W;
+        int hin = 1, hlast = 0;
+#pragma unroll(WT > 0 ? WT : 1)
+        for (int w = 0; w < nw; ++w) {
+            unsigned long long Eq = w < W ? eq[w] : 0ull;
+            const unsigned long long pv = Pv[w], mv = Mv[w];
+            const unsigned long long neg = hin < 0 ? 1ull : 0ull, pos = hin > 0 ? 1ull : 0ull;
+            const unsigned long long Xv = Eq | mv;
+            Eq |= neg;
+            const unsigned long long Xh = (((Eq & pv) + pv) ^ pv) | Eq;
+            unsigned long long Ph = mv | ~(Xh | pv);
+            unsigned long long Mh = pv & Xh;
+            const unsigned long long hb = (w == W - 1) ? last_bit : (1ull << 63);
+            const int hout = (Ph & hb) ? 1 : ((Mh & hb) ? -1 : 0);
+            Ph = (Ph << 1) | pos;
+            Mh = (Mh << 1) | neg;
+            Pv[w] = Mh | ~(Xv | Ph);
+            Mv[w] = Ph & Xv;
+            if (w == W - 1) hlast = hout;
+            hin = hout;
+        }
+        score += hlast;
+    }
+    return score;
+}
+
+// One thread per point, the centres in order; each centre's match vectors Peq[symbol][word]
+// are built once per block in shared memory.  `dist <= best` keeps the last of equal
+// distances, best starts at FLT_MAX and the cell at 0 (include/point.hpp:537-559).
+template <int WT>
+__global__ void __launch_bounds__(kVE) k_voronoi_edit(const uint8_t* __restrict__ atoms,
+                                                      const int64_t* __restrict__ off, int64_t n,
+                                                      const uint8_t* __restrict__ catoms,
+                                                      const int64_t* __restrict__ coff, int64_t m,
+                                                      int64_t* __restrict__ cell, float* __restrict__ dist)
+{
+    extern __shared__ unsigned long long peq[];  // 256 * Wmax words
+    const int64_t i = (int64_t)blockIdx.x * kVE + threadIdx.x;
+    const bool live = i < n;
+    const int64_t to = live ? off[i] : 0, lt = live ? off[i + 1] - to : 0;
+    const uint8_t* t = atoms + to;
+    float best = FLT_MAX;
+    int64_t bi = 0;
+    for (int64_t c = 0; c < m; ++c) {
+        const int64_t co = coff[c];
+        const int lp = (int)(coff[c + 1] - co);
+        const int W = (lp + 63) >> 6;
+        __syncthreads();  // previous centre's vectors are no longer read
+        for (int k = threadIdx.x; k < 256 * W; k += kVE) peq[k] = 0ull;
+        __syncthreads();
+        for (int k = threadIdx.x; k < lp; k += kVE)
+            atomicOr(&peq[(int)catoms[co + k] * W + (k >> 6)], 1ull << (k & 63));
+        __syncthreads();
+        if (live) {
+            const int dv = lp == 0 ? (int)lt : myers_distance<WT>(peq, W, lp, t, lt);
+            const float d = (float)dv;
+            if (d <= best) {
+                best = d;
+                bi = c;
+            }
+        }
+    }
+    if (live) {
+        cell[i] = bi;
+        dist[i] = best;
+    }
+}
+
+__global__ void k_max_len(const int64_t* __restrict__ off, int64_t m, unsigned long long* __restrict__ out)
+{
+    unsigned long long mx = 0;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < m; c += (int64_t)gridDim.x * blockDim.x)
+        mx = max(mx, (unsigned long long)(off[c + 1] - off[c]));
+    atomicMax(out, mx);
+}
+
 }  // namespace rnng
 
 using namespace rnng;
@@ -296,9 +404,7 @@ using namespace rnng;
 extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int64_t* offsets, const int64_t* ids,
                                    int64_t n, float radius, unsigned flags, rnng_edges* out)
 {
-    if (!c) return RNNG_ERR_INVALID;
-    try {
-        RNNG_CUDA(cudaSetDevice(c->device));
+    return guarded(c, [&] {
         RNNG_REQUIRE(out != nullptr, RNNG_ERR_INVALID, "out is null");
         std::memset(out, 0, sizeof(*out));
         RNNG_REQUIRE(n >= 0 && (n == 0 || (atoms && offsets)), RNNG_ERR_INVALID, "bad strings");
@@ -449,45 +555,72 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
                     sort_edges_uv(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m);
             }
         }
-        // deliver
-        out->count = m;
-        out->staged = 1;
-        if (flags & RNNG_OUTPUT_DEVICE) {
-            out->on_device = 1;
-            out->u = c->out_u.as<int64_t>();
-            out->v = c->out_v.as<int64_t>();
-            out->w = c->out_w.as<float>();
-        } else {
-            const size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1);
-            const size_t bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
-            DevBuf& slot = c->host_stage;
-            if (2 * bi + bf > slot.bytes) {
-                if (slot.ptr) cudaFreeHost(slot.ptr);
-                slot.ptr = nullptr;
-                slot.bytes = 0;
-                RNNG_CUDA(cudaMallocHost(&slot.ptr, 2 * bi + bf + 256));
-                slot.bytes = 2 * bi + bf + 256;
-            }
-            char* h = (char*)slot.ptr;
-            out->u = (int64_t*)h;
-            out->v = (int64_t*)(h + bi);
-            out->w = (float*)(h + 2 * bi);
-            if (m) {
-                RNNG_CUDA(cudaMemcpyAsync(out->u, c->out_u.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, s));
-                RNNG_CUDA(cudaMemcpyAsync(out->v, c->out_v.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, s));
-                RNNG_CUDA(cudaMemcpyAsync(out->w, c->out_w.ptr, sizeof(float) * m, cudaMemcpyDeviceToHost, s));
-            }
-        }
+        deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m, flags, out);
         RNNG_CUDA(cudaStreamSynchronize(s));
         c->stats.edges = m;
         c->stats.kernel_launches = c->launches;
-        c->last_error.clear();
-        return RNNG_OK;
-    } catch (const Error& e) {
-        c->last_error = e.msg;
-        return e.code;
-    } catch (...) {
-        c->last_error = "unknown error";
-        return RNNG_ERR_INVALID;
-    }
+    });
+}
+
+extern "C" int rnng_voronoi_edit(rnng_ctx* c, const uint8_t* atoms, const int64_t* offsets, int64_t n,
+                                 const uint8_t* catoms, const int64_t* coffsets, int64_t m, unsigned flags,
+                                 int64_t* cell, float* dist)
+{
+    return guarded(c, [&] {
+        RNNG_REQUIRE(n >= 0 && m >= 1, RNNG_ERR_INVALID, "bad sizes (need at least one centre)");
+        RNNG_REQUIRE((n == 0 || (atoms && offsets && cell && dist)) && catoms && coffsets, RNNG_ERR_INVALID,
+                     "null pointer");
+        c->stats = rnng_stats{};
+        c->launches = 0;
+        if (n == 0) return;
+        cudaStream_t s = c->stream;
+        const bool dev_in = flags & RNNG_INPUT_DEVICE;
+        const int64_t natoms = dev_in ? 0 : offsets[n], ncatoms = dev_in ? 0 : coffsets[m];
+        const int64_t* doff = (const int64_t*)upload(c, c->ids_in, offsets, sizeof(int64_t) * (n + 1), flags);
+        const uint8_t* datoms = (const uint8_t*)upload(c, c->x_in, atoms, (size_t)natoms, flags);
+        const int64_t* dcoff = (const int64_t*)upload(c, c->aux7, coffsets, sizeof(int64_t) * (m + 1), flags);
+        const uint8_t* dcatoms = (const uint8_t*)upload(c, c->pivots, catoms, (size_t)ncatoms, flags);
+        // longest centre: sizes the shared match vectors and picks the register variant
+        c->counters.reserve(sizeof(unsigned long long) * 16);
+        unsigned long long* dmax = c->counters.as<unsigned long long>() + 9;
+        RNNG_CUDA(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
+        k_max_len<<<(unsigned)std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 4), 256, 0, s>>>(dcoff, m,
+                                                                                                          dmax);
+        ++c->launches;
+        unsigned long long maxlen = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&maxlen, dmax, sizeof(maxlen), cudaMemcpyDeviceToHost, s));
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        const int Wmax = (int)((maxlen + 63) / 64);
+        RNNG_REQUIRE(Wmax <= kVEMaxW, RNNG_ERR_UNSUPPORTED, "centres longer than 4096 characters");
+        int64_t* dcell = cell;
+        float* ddist = dist;
+        if (!(flags & RNNG_OUTPUT_DEVICE)) {
+            c->out_u.reserve(sizeof(int64_t) * n);
+            c->out_w.reserve(sizeof(float) * n);
+            dcell = c->out_u.as<int64_t>();
+            ddist = c->out_w.as<float>();
+        }
+        const size_t smem = sizeof(unsigned long long) * 256 * (size_t)std::max(Wmax, 1);
+        const unsigned grid = (unsigned)ceil_div(n, kVE);
+        if (Wmax <= 1) {
+            k_voronoi_edit<1><<<grid, kVE, smem, s>>>(datoms, doff, n, dcatoms, dcoff, m, dcell, ddist);
+        } else if (Wmax <= 2) {
+            k_voronoi_edit<2><<<grid, kVE, smem, s>>>(datoms, doff, n, dcatoms, dcoff, m, dcell, ddist);
+        } else if (Wmax <= 4) {
+            k_voronoi_edit<4><<<grid, kVE, smem, s>>>(datoms, doff, n, dcatoms, dcoff, m, dcell, ddist);
+        } else {
+            if (smem > 48 * 1024)
+                RNNG_CUDA(cudaFuncSetAttribute(k_voronoi_edit<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem));
+            k_voronoi_edit<0><<<grid, kVE, smem, s>>>(datoms, doff, n, dcatoms, dcoff, m, dcell, ddist);
+        }
+        ++c->launches;
+        RNNG_CUDA(cudaGetLastError());
+        if (!(flags & RNNG_OUTPUT_DEVICE)) {
+            RNNG_CUDA(cudaMemcpyAsync(cell, dcell, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, s));
+            RNNG_CUDA(cudaMemcpyAsync(dist, ddist, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+        }
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        c->stats.kernel_launches = c->launches;
+    });
 }

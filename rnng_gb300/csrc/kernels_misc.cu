@@ -1,5 +1,8 @@
-// Device fault word and edge sorting shared by the pipelines.
+// Device fault word, edge sorting, uploads and result delivery shared by the pipelines.
 #include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstring>
 
 #include "kernels_misc.cuh"
 
@@ -64,6 +67,83 @@ void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m)
     RNNG_CUDA(cudaMemcpyAsync(v, kbuf, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
     k_gather<float><<<grid, 256, 0, s>>>(w, i0, wtmp, m); ++c->launches;
     RNNG_CUDA(cudaMemcpyAsync(w, wtmp, sizeof(float) * m, cudaMemcpyDeviceToDevice, s));
+}
+
+const void* upload(rnng_ctx* c, DevBuf& buf, const void* p, size_t bytes, unsigned flags)
+{
+    if (!p || (flags & RNNG_INPUT_DEVICE)) return p;
+    buf.reserve(std::max<size_t>(bytes, 1));
+    if (bytes) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, p, bytes, cudaMemcpyHostToDevice, c->stream));
+    return buf.ptr;
+}
+
+void* host_stage(rnng_ctx* c, size_t bytes)
+{
+    DevBuf& slot = c->host_stage;  // a DevBuf holding a cudaMallocHost block
+    if (bytes <= slot.bytes) return slot.ptr;
+    if (slot.ptr) {
+        RNNG_CUDA(cudaStreamSynchronize(c->stream));  // earlier copies may still target it
+        cudaFreeHost(slot.ptr);
+    }
+    slot.ptr = nullptr;
+    slot.bytes = 0;
+    const size_t grow = bytes + bytes / 4 + 256;
+    RNNG_CUDA(cudaMallocHost(&slot.ptr, grow));
+    slot.bytes = grow;
+    return slot.ptr;
+}
+
+void deliver_edges(rnng_ctx* c, const int64_t* du, const int64_t* dv, const float* dw, int64_t m, unsigned flags,
+                   rnng_edges* out)
+{
+    std::memset(out, 0, sizeof(*out));
+    out->count = m;
+    out->staged = 1;
+    if (flags & RNNG_OUTPUT_DEVICE) {
+        out->on_device = 1;
+        out->u = const_cast<int64_t*>(du);
+        out->v = const_cast<int64_t*>(dv);
+        out->w = const_cast<float*>(dw);
+        return;
+    }
+    const size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1);
+    const size_t bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
+    char* h = (char*)host_stage(c, 2 * bi + bf);
+    out->u = (int64_t*)h;
+    out->v = (int64_t*)(h + bi);
+    out->w = (float*)(h + 2 * bi);
+    if (m) {
+        RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
+        RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
+        RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream));
+    }
+}
+
+void deliver_simplices(rnng_ctx* c, const int64_t* did, const float* dval, const uint8_t* dflag, int64_t count,
+                       unsigned flags, rnng_simplices* out)
+{
+    std::memset(out, 0, sizeof(*out));
+    out->count = count;
+    out->staged = 1;
+    if (flags & RNNG_OUTPUT_DEVICE) {
+        out->on_device = 1;
+        out->id = const_cast<int64_t*>(did);
+        out->value = const_cast<float*>(dval);
+        out->flag = const_cast<uint8_t*>(dflag);
+        return;
+    }
+    const size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(count, 1);
+    const size_t bf = sizeof(float) * (size_t)std::max<int64_t>(count, 1);
+    const size_t bg = dflag ? (size_t)std::max<int64_t>(count, 1) : 0;
+    char* h = (char*)host_stage(c, bi + bf + bg);
+    out->id = (int64_t*)h;
+    out->value = (float*)(h + bi);
+    out->flag = dflag ? (uint8_t*)(h + bi + bf) : nullptr;
+    if (count) {
+        RNNG_CUDA(cudaMemcpyAsync(out->id, did, sizeof(int64_t) * count, cudaMemcpyDeviceToHost, c->stream));
+        RNNG_CUDA(cudaMemcpyAsync(out->value, dval, sizeof(float) * count, cudaMemcpyDeviceToHost, c->stream));
+        if (dflag) RNNG_CUDA(cudaMemcpyAsync(out->flag, dflag, (size_t)count, cudaMemcpyDeviceToHost, c->stream));
+    }
 }
 
 }  // namespace rnng

@@ -210,82 +210,12 @@ __global__ void k_mark_unique(const int64_t* __restrict__ u, const int64_t* __re
 
 using namespace rnng;
 
-namespace {
-
-template <class F>
-int guarded_call(rnng_ctx* ctx, F&& body)
-{
-    if (!ctx) return RNNG_ERR_INVALID;
-    try {
-        RNNG_CUDA(cudaSetDevice(ctx->device));
-        body();
-        ctx->last_error.clear();
-        return RNNG_OK;
-    } catch (const Error& e) {
-        ctx->last_error = e.msg;
-        return e.code;
-    } catch (...) {
-        ctx->last_error = "unknown error";
-        return RNNG_ERR_INVALID;
-    }
-}
-
-const void* upload(rnng_ctx* c, DevBuf& buf, const void* p, size_t bytes, unsigned flags)
-{
-    if (!p || (flags & RNNG_INPUT_DEVICE)) return p;
-    buf.reserve(std::max<size_t>(bytes, 1));
-    if (bytes) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, p, bytes, cudaMemcpyHostToDevice, c->stream));
-    return buf.ptr;
-}
-
-void* host_stage(rnng_ctx* c, size_t bytes)
-{
-    DevBuf& slot = c->host_stage;
-    if (bytes > slot.bytes) {
-        if (slot.ptr) cudaFreeHost(slot.ptr);
-        slot.ptr = nullptr;
-        slot.bytes = 0;
-        const size_t grow = bytes + bytes / 4 + 256;
-        RNNG_CUDA(cudaMallocHost(&slot.ptr, grow));
-        slot.bytes = grow;
-    }
-    return slot.ptr;
-}
-
-void give_edges(rnng_ctx* c, int64_t* du, int64_t* dv, float* dw, int64_t m, unsigned flags, rnng_edges* out)
-{
-    std::memset(out, 0, sizeof(*out));
-    out->count = m;
-    out->staged = 1;
-    if (flags & RNNG_OUTPUT_DEVICE) {
-        out->on_device = 1;
-        out->u = du;
-        out->v = dv;
-        out->w = dw;
-        return;
-    }
-    const size_t bi = sizeof(int64_t) * (size_t)std::max<int64_t>(m, 1);
-    const size_t bf = sizeof(float) * (size_t)std::max<int64_t>(m, 1);
-    char* h = (char*)host_stage(c, 2 * bi + bf);
-    out->u = (int64_t*)h;
-    out->v = (int64_t*)(h + bi);
-    out->w = (float*)(h + 2 * bi);
-    if (m) {
-        RNNG_CUDA(cudaMemcpyAsync(out->u, du, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
-        RNNG_CUDA(cudaMemcpyAsync(out->v, dv, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, c->stream));
-        RNNG_CUDA(cudaMemcpyAsync(out->w, dw, sizeof(float) * m, cudaMemcpyDeviceToHost, c->stream));
-    }
-    RNNG_CUDA(cudaStreamSynchronize(c->stream));
-}
-
-}  // namespace
-
 extern "C" {
 
 int rnng_radius_query_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n, const float* Q,
                          const int64_t* qids, int64_t nq, int64_t d, float radius, unsigned flags, rnng_edges* out)
 {
-    return guarded_call(c, [&] {
+    return guarded(c, [&] {
         RNNG_REQUIRE(out != nullptr, RNNG_ERR_INVALID, "out is null");
         std::memset(out, 0, sizeof(*out));
         RNNG_REQUIRE(n >= 0 && nq >= 0 && d >= 1, RNNG_ERR_INVALID, "bad sizes");
@@ -334,7 +264,8 @@ int rnng_radius_query_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_
             if (flags & RNNG_SORT_OUTPUT)
                 sort_edges_uv(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m);
         }
-        give_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m, flags, out);
+        deliver_edges(c, c->out_u.as<int64_t>(), c->out_v.as<int64_t>(), c->out_w.as<float>(), m, flags, out);
+        RNNG_CUDA(cudaStreamSynchronize(s));
         c->stats.edges = m;
         c->stats.kernel_launches = c->launches;
     });
@@ -343,7 +274,7 @@ int rnng_radius_query_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_
 int rnng_voronoi_l2(rnng_ctx* c, const float* X, int64_t n, const float* C, int64_t m, int64_t d, unsigned flags,
                     int64_t* cell, float* dist)
 {
-    return guarded_call(c, [&] {
+    return guarded(c, [&] {
         RNNG_REQUIRE(n >= 0 && m >= 1 && d >= 1, RNNG_ERR_INVALID, "bad sizes (need at least one centre)");
         RNNG_REQUIRE((n == 0 || (X && cell && dist)) && C, RNNG_ERR_INVALID, "null pointer");
         c->stats = rnng_stats{};
@@ -374,7 +305,7 @@ int rnng_voronoi_l2(rnng_ctx* c, const float* X, int64_t n, const float* C, int6
 
 int rnng_graph_finalize(rnng_ctx* c, const rnng_edges* edges, int64_t nv, unsigned flags, rnng_edges* out)
 {
-    return guarded_call(c, [&] {
+    return guarded(c, [&] {
         RNNG_REQUIRE(edges && out && nv >= 0 && edges->count >= 0, RNNG_ERR_INVALID, "bad arguments");
         std::memset(out, 0, sizeof(*out));
         c->stats = rnng_stats{};
@@ -408,7 +339,6 @@ int rnng_graph_finalize(rnng_ctx* c, const rnng_edges* edges, int64_t nv, unsign
             int64_t* cu = c->aux4.as<int64_t>();
             int64_t* cv = cu + total;
             float* cw = (float*)(cv + total);
-            int64_t* nsel = (int64_t*)(cw + total + (total & 1));
             c->aux3.reserve(sizeof(int64_t) * 4);
             size_t tmp = 0;
             int64_t* dsel = c->aux3.as<int64_t>();
@@ -418,14 +348,14 @@ int rnng_graph_finalize(rnng_ctx* c, const rnng_edges* edges, int64_t nv, unsign
             RNNG_CUDA(cub::DeviceSelect::Flagged(c->cub_tmp.ptr, tmp, ov, keep, cv, dsel, (int)total, s));
             RNNG_CUDA(cub::DeviceSelect::Flagged(c->cub_tmp.ptr, tmp, ow, keep, cw, dsel, (int)total, s));
             c->launches += 6;
-            (void)nsel;
             RNNG_CUDA(cudaMemcpyAsync(&kept, dsel, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
             RNNG_CUDA(cudaStreamSynchronize(s));
             RNNG_CUDA(cudaMemcpyAsync(ou, cu, sizeof(int64_t) * kept, cudaMemcpyDeviceToDevice, s));
             RNNG_CUDA(cudaMemcpyAsync(ov, cv, sizeof(int64_t) * kept, cudaMemcpyDeviceToDevice, s));
             RNNG_CUDA(cudaMemcpyAsync(ow, cw, sizeof(float) * kept, cudaMemcpyDeviceToDevice, s));
         }
-        give_edges(c, ou, ov, ow, kept, flags, out);
+        deliver_edges(c, ou, ov, ow, kept, flags, out);
+        RNNG_CUDA(cudaStreamSynchronize(s));
         c->stats.edges = kept;
         c->stats.kernel_launches = c->launches;
     });

@@ -15,9 +15,19 @@ Fixtures (npz, inputs + expected):
   k2_landmark   integer descriptors 0..255, 1200 x 128 (stored as uint8)
   k3_edit       DNA families, 300 strings, radius 8, landmark path with edit distance
   k4_rips       torus in R^16, 1200 points, maxdim 2, rips path
+  k4_rips3      torus in R^16, 600 points, maxdim 3 (the rips driver's default)
+  k3_rips_edit  DNA families, 96 strings, radius 8, maxdim 2, rips path with edit distance
   k5_landmark   Zipf Gaussian mixture, 2500 x 32
+  k1_cells      the k1 input's Voronoi cells (30 landmarks) after coalescing, with the
+                landmark driver's ghosts; k1_cells_rips with the rips driver's ghosts
+                and interior flags
+  k3_cells      the k3 strings' cells (30 landmarks) with the rips driver's ghosts
+  dup_cells     400 points on 60 distinct positions in R^4, 40 landmarks: identical
+                landmarks leave cells empty
 Edge fixtures hold the unordered edge set (u < v) with weights, and the driver's
-reported edge count (n + 2|E|); the Rips fixture holds the merged filtration.
+reported edge count (n + 2|E|); the Rips fixtures hold the merged filtration; the cell
+fixtures hold per cell its id, point ids, distances to the centre, interior flags and
+ghost ids, in RNNG's order.
 """
 from __future__ import annotations
 
@@ -53,6 +63,26 @@ def edges_fixture(name, tmp, mode, path_in, radius, extra, n, save_inputs):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), radius=np.float32(radius), u=eu, v=ev, w=ew,
                         reported_edges=np.int64(full), n=np.int64(n), **save_inputs)
     print(f"{name}: n={n} |E|={eu.size} reported={full}")
+
+
+def cells_fixture(name, tmp, metric, path_in, radius, m, seed, rips, save_inputs):
+    out = os.path.join(tmp, name + ".bin")
+    run(["cells", metric, path_in, repr(float(radius)), m, seed, 1 if rips else 0, out])
+    cells = oracle.read_cells_dump(out)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), radius=np.float32(radius), m=np.int64(m),
+                        seed=np.int64(seed), rips=np.int64(1 if rips else 0), **cells, **save_inputs)
+    empty = int((cells["npts"] == 0).sum())
+    print(f"{name}: cells={cells['npts'].size} empty={empty} ghosts={cells['ghosts'].size}")
+
+
+def rips_fixture(name, tmp, metric, path_in, radius, maxdim, m, seed, n, save_inputs):
+    out = os.path.join(tmp, name + ".bin")
+    run(["rips", metric, path_in, repr(float(radius)), maxdim, m, seed, out])
+    ids, vals = oracle.read_simplex_dump(out)
+    mids, mvals = oracle.merge_filtration(ids, vals)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), radius=np.float32(radius), ids=mids, values=mvals,
+                        maxdim=np.int64(maxdim), n=np.int64(n), **save_inputs)
+    print(f"{name}: n={n} simplices={mids.size}")
 
 
 def main():
@@ -93,14 +123,33 @@ def main():
         e4 = synth.choose_eps(x4, 15.0, sample=1200)
         p4 = os.path.join(tmp, "k4.fvecs")
         synth.write_fvecs(p4, x4)
-        out = os.path.join(tmp, "k4.bin")
-        run(["rips", p4, repr(float(e4)), 2, 24, 7, out])
-        ids, vals = oracle.read_simplex_dump(out)
-        mids, mvals = oracle.merge_filtration(ids, vals)
-        np.savez_compressed(os.path.join(HERE, "k4_rips.npz"), radius=np.float32(e4), x=x4, ids=mids, values=mvals,
-                            maxdim=np.int64(2), n=np.int64(1200))
-        print(f"k4_rips: n=1200 simplices={mids.size}")
+        rips_fixture("k4_rips", tmp, "l2", p4, e4, 2, 24, 7, 1200, {"x": x4})
 
+        # K4-like at the rips driver's default dimension 3
+        x43 = synth.torus16(n=600, seed=44)
+        e43 = synth.choose_eps(x43, 12.0, sample=600)
+        p43 = os.path.join(tmp, "k43.fvecs")
+        synth.write_fvecs(p43, x43)
+        rips_fixture("k4_rips3", tmp, "l2", p43, e43, 3, 12, 7, 600, {"x": x43})
+
+        # Rips over edit distance
+        seqs_r = synth.dna_families(n_seeds=12, mutants=8, seed=33)
+        p3r = os.path.join(tmp, "k3r.seqs")
+        synth.write_seqs(p3r, seqs_r)
+        atoms_r, offsets_r = synth.pack_seqs(seqs_r)
+        rips_fixture("k3_rips_edit", tmp, "edit", p3r, np.float32(8.0), 2, 10, 7, len(seqs_r),
+                     {"atoms": atoms_r, "offsets": offsets_r})
+
+        # Voronoi cells and ghosts
+        cells_fixture("k1_cells", tmp, "l2", p1, np.float32(1.5), 30, 7, False, {"x": x1})
+        cells_fixture("k1_cells_rips", tmp, "l2", p1, np.float32(1.5), 30, 7, True, {"x": x1})
+        cells_fixture("k3_cells", tmp, "edit", p3, np.float32(8.0), 30, 7, True, {"atoms": atoms, "offsets": offsets})
+        rng = np.random.default_rng(12)
+        base = rng.normal(size=(60, 4)).astype(np.float32) * np.float32(2.0)
+        xd = base[rng.integers(0, 60, size=400)]
+        pd = os.path.join(tmp, "dup.fvecs")
+        synth.write_fvecs(pd, xd)
+        cells_fixture("dup_cells", tmp, "l2", pd, np.float32(3.0), 40, 11, True, {"x": xd})
 
 if __name__ == "__main__":
     main()

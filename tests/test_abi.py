@@ -32,3 +32,25 @@ def test_context_without_gpu_fails_cleanly():
     import rnng_gb300
     with pytest.raises(rnng_gb300.RnngError):
         rnng_gb300.Context(0)
+
+
+def test_dropin_harness_builds_against_the_dropin_headers():
+    """The harness source that makes RNNG's API calls compiles against include/*.h and
+    links to librnng_gpu.so (it runs in the GPU tests)."""
+    import subprocess
+    import rnng_gb300
+    rnng_gb300.build.build()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin"], check=True)
+    assert os.path.exists(os.path.join(ROOT, "oracle", "_build", "dropin_harness"))
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/drivers"), reason="needs the RNNG driver sources")
+def test_unchanged_reference_drivers_build_against_the_dropin_headers():
+    """drivers/systolic.cpp, landmark.cpp and rips.cpp, unmodified, compile against the
+    drop-in headers and link to librnng_gpu.so and the single-rank MPI shim."""
+    import subprocess
+    import rnng_gb300
+    rnng_gb300.build.build()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin-drivers"], check=True)
+    for d in ("systolic", "landmark", "rips"):
+        assert os.path.exists(os.path.join(ROOT, "oracle", "_build", "dropin_" + d))

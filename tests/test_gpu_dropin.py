@@ -1,0 +1,88 @@
+"""The drop-in headers (include/*.h) against RNNG's own outputs.
+
+oracle/ref_harness.cpp makes the drivers' API calls (PointContainer, selection_sample,
+VoronoiDiagram, coalesce_cells, the ghost steps, CoverTree searches, VoronoiComplex)
+and dumps their results.  Compiled against RNNG's headers it made the golden fixtures;
+here the same source is compiled against the drop-in headers and linked to
+librnng_gpu.so, and every dump must equal the fixture bit for bit."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, golden_points
+
+pytestmark = pytest.mark.gpu
+
+HARNESS = os.path.join(ROOT, "oracle", "_build", "dropin_harness")
+
+
+@pytest.fixture(scope="module")
+def harness(ctx):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin"], check=True)
+    return HARNESS
+
+
+def run(harness, *args):
+    subprocess.run([harness] + [str(a) for a in args], check=True, capture_output=True, timeout=600)
+
+
+def write_input(tmp_path, g):
+    from rnng_gb300 import synth
+    if "atoms" in g:
+        atoms, offsets = g["atoms"], g["offsets"]
+        seqs = [atoms[offsets[i]:offsets[i + 1]].tobytes() for i in range(offsets.size - 1)]
+        path = str(tmp_path / "in.seqs")
+        synth.write_seqs(path, seqs)
+        return "edit", path
+    path = str(tmp_path / "in.fvecs")
+    synth.write_fvecs(path, golden_points(g))
+    return "l2", path
+
+
+def assert_edges(orc, dump, g):
+    u, v, w = orc.read_edge_dump(dump)
+    eu, ev, ew, full = orc.reference_graph_semantics(u, v, w)
+    assert np.array_equal(eu, g["u"]) and np.array_equal(ev, g["v"])
+    assert np.array_equal(ew.view(np.uint32), g["w"].view(np.uint32))
+    assert full == int(g["reported_edges"])
+
+
+def test_systolic_k1(harness, orc, tmp_path):
+    g = golden("k1_systolic")
+    _, path = write_input(tmp_path, g)
+    out = str(tmp_path / "out.bin")
+    run(harness, "systolic", path, repr(float(g["radius"])), out)
+    assert_edges(orc, out, g)
+
+
+@pytest.mark.parametrize("name,m", [("k1_landmark", 30), ("k2_landmark", 12), ("k3_edit", 30), ("k5_landmark", 40)])
+def test_landmark(harness, orc, tmp_path, name, m):
+    g = golden(name)
+    metric, path = write_input(tmp_path, g)
+    out = str(tmp_path / "out.bin")
+    run(harness, "landmark", metric, path, repr(float(g["radius"])), m, 7, out)
+    assert_edges(orc, out, g)
+
+
+@pytest.mark.parametrize("name", ["k1_cells", "k1_cells_rips", "k3_cells", "dup_cells"])
+def test_cells_and_ghosts(harness, orc, tmp_path, name):
+    g = golden(name)
+    metric, path = write_input(tmp_path, g)
+    out = str(tmp_path / "out.bin")
+    run(harness, "cells", metric, path, repr(float(g["radius"])), int(g["m"]), int(g["seed"]), int(g["rips"]), out)
+    got = orc.read_cells_dump(out)
+    for k in got:
+        assert np.array_equal(got[k], g[k]), k
+
+
+@pytest.mark.parametrize("name,m", [("k4_rips", 24), ("k4_rips3", 12), ("k3_rips_edit", 10)])
+def test_rips(harness, orc, tmp_path, name, m):
+    g = golden(name)
+    metric, path = write_input(tmp_path, g)
+    out = str(tmp_path / "out.bin")
+    run(harness, "rips", metric, path, repr(float(g["radius"])), int(g["maxdim"]), m, 7, out)
+    ids, vals = orc.merge_filtration(*orc.read_simplex_dump(out))
+    assert np.array_equal(ids, g["ids"])
+    assert np.array_equal(vals.view(np.uint32), g["values"].view(np.uint32))

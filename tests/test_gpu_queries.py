@@ -59,3 +59,32 @@ def test_graph_finalize_matches_reference_semantics(ctx, orc):
     o = np.lexsort((rv, ru))
     assert np.array_equal(fu, ru[o]) and np.array_equal(fv, rv[o])
     assert np.array_equal(fw.view(np.uint32), rw[o].view(np.uint32))
+
+
+@pytest.mark.parametrize("m", [1, 7, 30])
+def test_voronoi_edit_matches_oracle(ctx, orc, m):
+    from rnng_gb300 import synth
+    seqs = synth.dna_families(n_seeds=40, mutants=12, seed=m)
+    atoms, offsets = synth.pack_seqs(seqs)
+    rng = np.random.default_rng(m)
+    lm = np.sort(rng.choice(len(seqs), size=m, replace=False))
+    cseqs = [seqs[i] for i in lm]
+    catoms, coffsets = synth.pack_seqs(cseqs)
+    cell, dist = ctx.voronoi_edit((atoms, offsets), (catoms, coffsets))
+    wc, wd = orc.voronoi_edit(atoms, offsets, catoms, coffsets)
+    assert np.array_equal(cell, wc) and np.array_equal(dist, wd)
+
+
+def test_voronoi_edit_long_and_empty_strings(ctx, orc):
+    """Centres of 0 to 700 characters (1..11 words), ties between equal centres."""
+    rng = np.random.default_rng(5)
+    alphabet = np.frombuffer(b"ACGTN", np.uint8)
+    seqs = [bytes(rng.choice(alphabet, size=int(rng.integers(0, 700)))) for _ in range(300)] + [b""]
+    centres = [b"", seqs[3], seqs[3], bytes(rng.choice(alphabet, size=700)), seqs[10][:64], seqs[11][:65]]
+    import rnng_gb300
+    atoms, offsets = rnng_gb300._csr(seqs)
+    catoms, coffsets = rnng_gb300._csr(centres)
+    cell, dist = ctx.voronoi_edit((atoms, offsets), (catoms, coffsets))
+    wc, wd = orc.voronoi_edit(atoms, offsets, catoms, coffsets)
+    assert np.array_equal(cell, wc) and np.array_equal(dist, wd)
+    assert cell[3] == 2  # equal centres: the last wins

@@ -20,6 +20,94 @@ def test_golden_k4(ctx, mode):
     assert same(got, (g["ids"], g["values"]))
 
 
+@pytest.mark.parametrize("mode", ["fp32", "bf16"])
+def test_golden_k4_maxdim3(ctx, mode):
+    """The rips driver's default dimension (tetrahedra) against RNNG's own output."""
+    g = golden("k4_rips3")
+    got = ctx.rips_l2(g["x"], g["radius"], maxdim=3, mode=mode)
+    assert same(got, (g["ids"], g["values"]))
+
+
+def test_golden_edit_rips_through_edges(ctx):
+    """Edit-distance complex: the GPU edit epsilon graph fed to rnng_rips_edges equals
+    RNNG's rips path with EditDistance."""
+    g = golden("k3_rips_edit")
+    u, v, w = ctx.eps_graph_edit((g["atoms"], g["offsets"]), g["radius"])
+    got = ctx.rips_edges(int(g["n"]), u, v, w, maxdim=int(g["maxdim"]))
+    assert same(got, (g["ids"], g["values"]))
+
+
+@pytest.mark.parametrize("maxdim", [3, 4, 6])
+def test_higher_dimensions_against_oracle(ctx, orc, maxdim):
+    rng = np.random.default_rng(maxdim + 70)
+    x = rng.normal(size=(700, 3)).astype(np.float32)
+    r = np.float32(0.8)
+    u, v, w = orc.eps_graph_l2(x, r)
+    want = orc.rips(x.shape[0], u, v, w, maxdim)
+    got = ctx.rips_l2(x, r, maxdim=maxdim, mode="fp32")
+    assert same(got, want)
+    # RNNG's Binom wraps its 64-bit falling product (700 * 699 * ... beyond 6 factors), so
+    # ids of 7-vertex simplices here carry wrapped bits, identically on both sides;
+    # below that the dimension field decodes
+    decodable = maxdim <= 4
+    if decodable:
+        dims = want[0].view(np.uint64) >> np.uint64(60)
+        assert int(dims.max()) == maxdim
+    # the same complex from the edge list, rows permuted and edges in both orientations
+    perm = rng.permutation(x.shape[0])
+    inv = np.argsort(perm)
+    flip = rng.random(u.size) < 0.5
+    uu, vv = np.where(flip, inv[v], inv[u]), np.where(flip, inv[u], inv[v])
+    got2 = ctx.rips_edges(x.shape[0], uu, vv, w, maxdim=maxdim, ids=perm.astype(np.int64))
+    assert same(got2, want)
+    # per-simplex flags: the OR of its vertices' flags (RNNG's interior)
+    vflag = (rng.random(x.shape[0]) < 0.3).astype(np.uint8)
+    gi, gv, gf = ctx.rips_edges(x.shape[0], uu, vv, w, maxdim=maxdim, ids=perm.astype(np.int64),
+                                vertex_flags=vflag)
+    assert same((gi, gv), want)
+    if not decodable:
+        return
+    flag_of_id = np.zeros(x.shape[0], np.uint8)
+    flag_of_id[perm] = vflag
+    want_f = [max(flag_of_id[vtx] for vtx in _verts(int(i))) for i in gi]
+    assert gf.tolist() == want_f
+
+
+def _verts(sid: int) -> list[int]:
+    """Vertices of a simplex id (sum of C(v_i, i+1) over sorted v, dim << 60)."""
+    from math import comb
+    dim, rest = sid >> 60, sid & ((1 << 60) - 1)
+    out = []
+    for i in range(dim, -1, -1):
+        lo, hi = i, 1 << 21  # largest v with C(v, i+1) <= rest
+        while lo < hi:
+            mid = (lo + hi + 1) // 2
+            if comb(mid, i + 1) <= rest:
+                lo = mid
+            else:
+                hi = mid - 1
+        out.append(lo)
+        rest -= comb(lo, i + 1)
+    assert rest == 0
+    return out[::-1]
+
+
+def test_rips_edges_rejects_bad_graphs(ctx):
+    import rnng_gb300
+    with pytest.raises(rnng_gb300.RnngError):
+        ctx.rips_edges(3, [0, 1], [1, 0], [1.0, 1.0])  # the same pair twice
+    with pytest.raises(rnng_gb300.RnngError):
+        ctx.rips_edges(3, [0], [0], [1.0])  # self-loop
+    with pytest.raises(rnng_gb300.RnngError):
+        ctx.rips_edges(3, [0], [3], [1.0])  # row out of range
+    with pytest.raises(rnng_gb300.RnngError):
+        ctx.rips_edges(3, [0], [1], [-1.0])  # negative value
+    with pytest.raises(rnng_gb300.RnngError):
+        ctx.rips_l2(np.zeros((4, 2), np.float32), 1.0, maxdim=16)
+    ids, vals = ctx.rips_edges(4, [], [], [], maxdim=3)
+    assert ids.tolist() == [0, 1, 2, 3] and np.all(vals == 0)
+
+
 @pytest.mark.parametrize("maxdim", [0, 1, 2])
 def test_random_against_oracle(ctx, orc, maxdim):
     rng = np.random.default_rng(maxdim + 50)

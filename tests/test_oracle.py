@@ -31,12 +31,48 @@ def test_oracle_edit_matches_reference(orc):
     assert int(g["reported_edges"]) == int(g["n"]) + 2 * u.size
 
 
-def test_oracle_rips_matches_reference(orc):
-    g = golden("k4_rips")
-    u, v, w = orc.eps_graph_l2(g["x"], g["radius"])
+@pytest.mark.parametrize("name", ["k4_rips", "k4_rips3", "k3_rips_edit"])
+def test_oracle_rips_matches_reference(orc, name):
+    g = golden(name)
+    if "atoms" in g:
+        u, v, w = orc.eps_graph_edit(g["atoms"], g["offsets"], g["radius"])
+    else:
+        u, v, w = orc.eps_graph_l2(g["x"], g["radius"])
     ids, vals = orc.rips(int(g["n"]), u, v, w, int(g["maxdim"]))
     assert np.array_equal(ids, g["ids"])
     assert np.array_equal(vals.view(np.uint32), g["values"].view(np.uint32))
+    dims = np.asarray(g["ids"]).view(np.uint64) >> np.uint64(60)
+    assert int(dims.max()) == int(g["maxdim"])  # the top dimension is populated
+
+
+CELL_FIXTURES = ["k1_cells", "k1_cells_rips", "k3_cells", "dup_cells"]
+
+
+@pytest.mark.parametrize("name", CELL_FIXTURES)
+def test_oracle_cells_match_reference(orc, name):
+    """Voronoi assignment, coalescing, ghosts and interior flags restated in Python
+    (oracle.landmark_cells) equal RNNG's, including its empty-cell indexing."""
+    g = golden(name)
+    metric = "edit" if "atoms" in g else "l2"
+    data = (g["atoms"], g["offsets"]) if metric == "edit" else g["x"]
+    r = orc.landmark_cells(metric, data, g["landmarks"], g["radius"], bool(g["rips"]))
+    for k in r:
+        assert np.array_equal(r[k], g[k]), k
+    if name == "dup_cells":
+        assert (g["npts"] == 0).sum() > 0 and g["ghosts"].size > 0
+
+
+def test_oracle_voronoi_edit_matches_reference(orc):
+    g = golden("k3_cells")
+    lm = g["landmarks"]
+    atoms, offsets = g["atoms"], g["offsets"]
+    catoms = np.concatenate([atoms[offsets[i]:offsets[i + 1]] for i in lm])
+    coffsets = np.concatenate([[0], np.cumsum([offsets[i + 1] - offsets[i] for i in lm])]).astype(np.int64)
+    cell, dist = orc.voronoi_edit(atoms, offsets, catoms, coffsets)
+    want_cell = np.repeat(g["cell_id"], g["npts"])
+    order = np.argsort(g["ids"])
+    assert np.array_equal(cell, want_cell[order])
+    assert np.array_equal(dist, g["dist"][order])
 
 
 def _lev(s, t):

@@ -35,14 +35,15 @@ UNIT = "edges/s"
 N_POINTS, DIM = 1_000_000, 128
 
 
-def workload():
+def workload(n=N_POINTS):
     from rnng_gb300 import synth
-    return synth.descriptor(n=N_POINTS, d=DIM), synth.EPS_K2
+    return synth.descriptor(n=n, d=DIM), synth.EPS_K2
 
 
-def config(extra=None):
+def config(extra=None, n=N_POINTS):
     from rnng_gb300 import synth
-    c = {"workload": "k2-descriptors-1Mx128-f32", "points": N_POINTS, "dim": DIM,
+    name = "k2-descriptors-1Mx128-f32" if n == N_POINTS else f"k2-descriptors-{n}x128-f32 (profiling size)"
+    c = {"workload": name, "points": n, "dim": DIM,
          "radius": float(synth.EPS_K2), "radius_hex": hex(int(np.float32(synth.EPS_K2).view(np.uint32))),
          "clusters": 1000, "values": "integers 0..255 stored as float32",
          "l2_flush": "not needed: inputs (512 MB) larger than L2 (129 MB)"}
@@ -154,6 +155,8 @@ def main():
     ap.add_argument("--fp32-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--points", type=int, default=N_POINTS,
+                    help="points of the descriptor workload (smaller sizes are for ncu captures only)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -173,7 +176,7 @@ def main():
         dist.init_process_group("nccl", init_method="env://")
 
     import rnng_gb300
-    x, radius = workload()
+    x, radius = workload(args.points)
     n, d = x.shape
     ctx = rnng_gb300.Context(local)
     xd = torch.from_numpy(x).to(f"cuda:{local}")
@@ -255,7 +258,7 @@ def main():
     pairs = last["pairs_evaluated"]
     g_ms = statistics.median(gram_ms)
     achieved = 2.0 * d * pairs / (g_ms / 1e3) / 1e12
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic() if n == N_POINTS else None  # the committed capture is of the 1M workload
     roofline = {"bound": "tensor", "kernel": "k_gram_bf16", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
                 "flops_per_launch": 2.0 * d * pairs, "ms_per_launch": g_ms,
@@ -279,7 +282,7 @@ def main():
                                   "candidates": int(last["candidates"]),
                                   "stage_ms": {k: round(last[k], 3) for k in
                                                ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles", "ms_recheck",
-                                                "ms_finalize")}}),
+                                                "ms_finalize")}}, n),
                 "fp32_direct": fp32, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "gpu_launches": int(sum(launches)), "clocks": clk}
         print(json.dumps(line), flush=True)
@@ -304,7 +307,7 @@ def run_reference(args, world, rank):
     """Reference arm: RNNG's CPU path restated by the oracle, timed on the host cores."""
     if rank != 0:
         return
-    x, radius = workload()
+    x, radius = workload(args.points)
     n = x.shape[0]
     vals = []
     for i in range(args.warmup + args.steps):
@@ -317,7 +320,7 @@ def run_reference(args, world, rank):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
-            "config": config(), "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+            "config": config(n=n), "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": leg["cores"], "kind": "port",
                              "sample": f"{leg['rows']} strided query rows x all {n} points per step"}}

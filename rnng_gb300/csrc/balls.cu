@@ -452,36 +452,42 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
     }
 }
 
-// Schedule key of a tile pair for the tile kernels: (i mod G, i, j), so that after a
-// sort the pairs of CTA g (row tiles i = g, g + G, ...) are contiguous, each row's
-// column tiles ascend and CTAs sweep the same column tiles at about the same time.
-__global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, int G, uint64_t* __restrict__ keys)
+// Schedule of the tile pairs for the persistent Gram kernel.  The pairs are sorted by
+// (row tile, column tile) and cut into chunks of kSchedChunk; chunk k goes to CTA k mod G.
+// Every CTA gets the same number of pairs (within one chunk), all CTAs work on
+// neighbouring rows at any moment (their B tiles are shared through L2), and a CTA
+// reloads its resident A tile at most once per chunk.  Each CTA's chunks are stored
+// contiguously, so the kernel reads one range per CTA.
+__global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, uint64_t* __restrict__ keys)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
         const int2 q = pairs[p];
-        keys[p] = ((uint64_t)(q.x % G) << 42) | ((uint64_t)q.x << 21) | (uint64_t)q.y;
+        keys[p] = ((uint64_t)q.x << 21) | (uint64_t)q.y;
     }
 }
 
-__global__ void k_schedule_unpack(const uint64_t* __restrict__ keys, int64_t m, int2* __restrict__ pairs,
-                                  unsigned long long* __restrict__ starts)
+__global__ void k_schedule_scatter(const uint64_t* __restrict__ keys, int64_t m, int G,
+                                   const unsigned long long* __restrict__ starts, int2* __restrict__ pairs)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
         const uint64_t k = keys[p];
-        pairs[p] = make_int2((int)((k >> 21) & 0x1fffff), (int)(k & 0x1fffff));
-        const uint64_t g = k >> 42;
-        if (p == 0 || (keys[p - 1] >> 42) != g) starts[g] = (unsigned long long)p;
+        const int64_t chunk = p / kSchedChunk;
+        const int g = (int)(chunk % G);
+        const int64_t dest = (int64_t)starts[g] + (chunk / G) * kSchedChunk + p % kSchedChunk;
+        pairs[dest] = make_int2((int)(k >> 21), (int)(k & 0x1fffff));
     }
-}
-
-__global__ void k_schedule_fix(unsigned long long* __restrict__ starts, int G)
-{
-    // CTAs without pairs get an empty range: starts[g] = starts[g + 1]
-    for (int g = G - 1; g >= 0; --g) starts[g] = min(starts[g], starts[g + 1]);
 }
 
 // ------------------------------------------------------------------------------------------------
 // host
+
+// Bits of the largest tile index (at least 1).
+static int bits_for_tiles(int64_t T)
+{
+    int b = 1;
+    while (b < 63 && (int64_t(1) << b) < T) ++b;
+    return b;
+}
 
 void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchild, const int32_t* child_off,
                   int ncells, int32_t* rank)
@@ -564,9 +570,15 @@ void schedule_pairs(rnng_ctx* c, Layout& L, int G)
     unsigned long long* starts = c->sched.as<unsigned long long>();
     L.sched = starts;
     L.sched_G = G;
-    // every CTA's range starts empty (= m) until a boundary sets it
-    std::vector<unsigned long long> init(G + 1, (unsigned long long)m);
-    RNNG_CUDA(cudaMemcpyAsync(starts, init.data(), sizeof(unsigned long long) * (G + 1), cudaMemcpyHostToDevice, s));
+    // segment of CTA g: its chunks k = g, g + G, ... (all full but the very last chunk)
+    const int64_t nchunks = ceil_div(m, kSchedChunk), tail = m % kSchedChunk;
+    std::vector<unsigned long long> h(G + 1, 0);
+    for (int g = 0; g < G; ++g) {
+        int64_t size = (nchunks / G + (g < nchunks % G ? 1 : 0)) * kSchedChunk;
+        if (tail > 0 && (nchunks - 1) % G == g) size -= kSchedChunk - tail;
+        h[g + 1] = h[g] + (unsigned long long)size;
+    }
+    RNNG_CUDA(cudaMemcpyAsync(starts, h.data(), sizeof(unsigned long long) * (G + 1), cudaMemcpyHostToDevice, s));
     if (m == 0) {
         RNNG_CUDA(cudaStreamSynchronize(s));
         return;
@@ -576,14 +588,14 @@ void schedule_pairs(rnng_ctx* c, Layout& L, int G)
     uint64_t* k0 = c->aux6.as<uint64_t>();
     uint64_t* k1 = k0 + m;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
-    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, G, k0); ++c->launches;
+    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, k0); ++c->launches;
     size_t tmp = 0;
-    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, 64, s));
+    const int bits = 21 + bits_for_tiles(L.T);
+    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, bits, s));
     c->cub_tmp.reserve(tmp);
-    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, 64, s)); c->launches += cub_sort_kernels(m, 64);
-    k_schedule_unpack<<<grid, 256, 0, s>>>(k1, m, L.pairs, starts); ++c->launches;
-    k_schedule_fix<<<1, 1, 0, s>>>(starts, G); ++c->launches;
-    RNNG_CUDA(cudaStreamSynchronize(s));  // init lifetime
+    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, bits, s)); c->launches += cub_sort_kernels(m, bits);
+    k_schedule_scatter<<<grid, 256, 0, s>>>(k1, m, G, starts, L.pairs); ++c->launches;
+    RNNG_CUDA(cudaStreamSynchronize(s));  // h lifetime
 }
 
 }  // namespace rnng

@@ -13,6 +13,7 @@ constexpr int kBalls = 4;           // balls covering one tile (and one super-ti
 constexpr int kFan = 64;            // children per split of the landmark partition
 constexpr int64_t kLeafTarget = 128;  // points per leaf cell
 constexpr int kMaxLevels = 8;       // depth limit of the partition
+constexpr int64_t kSchedChunk = 64;  // consecutive tile pairs a Gram CTA takes at a time
 
 // Device layout of one epsilon-graph problem after the partition.
 struct Layout {

@@ -249,11 +249,11 @@ struct PairPrefetch {
 // ------------------------------------------------------------------------------------------------
 // the Gram kernel
 //
-// CTA g takes its range of the scheduled tile-pair list: row tiles i = g, g + G, ...
-// in order, each with its column tiles ascending.  The A tile (rows of i, all
-// K-chunks) stays resident in shared memory for the whole row, only B tiles stream
-// through the ring, and all CTAs sweep similar column tiles at the same time so
-// that B tiles are shared through L2.
+// CTA g takes its range of the scheduled tile-pair list: the chunks g, g + G, ... of
+// the pairs sorted by (row tile, column tile).  The A tile (rows of i, all K-chunks)
+// stays resident in shared memory while the row lasts, only B tiles stream through
+// the ring, and all CTAs work on neighbouring rows at the same time so that B tiles
+// are shared through L2.
 
 __global__ void __launch_bounds__(kGramThreads, 1)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int2* __restrict__ pairs,

@@ -42,7 +42,6 @@ namespace rnng {
 constexpr int kChunkK = 64;                         // BF16 elements per K-chunk (one 128 B swizzle span)
 constexpr int kChunkBytes = kTile * kChunkK * 2;    // 16 KB per operand tile per chunk
 constexpr int kMaxDp = 256;                         // padded dimension limit of the BF16 path
-constexpr int kRingBytes = 8 * kChunkBytes;         // B-operand ring: item slots of kchunks chunks
 constexpr int kMaxSlots = 8;
 constexpr int kAccCols = 128;                       // fp32 accumulator columns (N)
 constexpr int kAccBufs = 4;                         // accumulators in tensor memory
@@ -53,16 +52,31 @@ constexpr int kEpiWarps = kEpiGroups * kGroupWarps;
 constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 576
 constexpr int kEpiCols = kAccCols / (kGroupWarps / 4);  // accumulator columns per epilogue warp (64)
 constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
+constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared memory per block (227 KB)
 
+// Offsets inside the dynamic shared block (aligned to 1024 bytes in the kernel): the
+// small parts first, then the resident A tile (kchunks chunks) and as many B item slots
+// of kchunks chunks as the rest of the 227 KB holds.  Operand tiles start on 1024-byte
+// boundaries (128-byte swizzle atoms).
 struct GramSmem {
-    // offsets inside the dynamic shared block (which is 1024-aligned)
-    static constexpr int a_tile = 0;                                    // resident A tile, kMaxDp/64 chunks
-    static constexpr int b_ring = (kMaxDp / kChunkK) * kChunkBytes;     // B item slots
-    static constexpr int colinfo = b_ring + kRingBytes;                 // kEpiWarps x kEpiCols floats (u_j)
-    static constexpr int bars = colinfo + kEpiWarps * kEpiCols * 4;     // mbarriers
+    uint32_t colinfo, bars, misc, a_tile, b_ring, slot_bytes, total;
+    int nslots;
     static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1;  // a_full/empty, b_full/empty, tfull/tempty, drain
-    static constexpr int misc = bars + nbars * 8;                       // tmem slot, abort flag
-    static constexpr int total = misc + 16;
+    __host__ __device__ static GramSmem make(int kchunks)
+    {
+        GramSmem g;
+        g.colinfo = 0;                                     // kEpiWarps x kEpiCols floats (u_j)
+        g.bars = g.colinfo + kEpiWarps * kEpiCols * 4;     // mbarriers
+        g.misc = g.bars + nbars * 8;                       // tmem slot, abort flag
+        g.a_tile = (g.misc + 16 + 1023) & ~1023u;
+        g.slot_bytes = (uint32_t)kchunks * kChunkBytes;
+        g.b_ring = g.a_tile + g.slot_bytes;
+        const uint32_t room = kSmemLimit - 1024 - g.b_ring;  // 1024: alignment slack of the block base
+        g.nslots = (int)(room / g.slot_bytes);
+        if (g.nslots > kMaxSlots) g.nslots = kMaxSlots;
+        g.total = g.b_ring + (uint32_t)g.nslots * g.slot_bytes;
+        return g;
+    }
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -255,9 +269,10 @@ struct PairPrefetch {
 // the ring, and all CTAs work on neighbouring rows at the same time so that B tiles
 // are shared through L2.
 
+template <int KCH>  // K-chunks of 64 dimensions: dp = 64 KCH
 __global__ void __launch_bounds__(kGramThreads, 1)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int2* __restrict__ pairs,
-                const unsigned long long* __restrict__ npairs_ptr, unsigned long long pair_cap, int kchunks,
+                const unsigned long long* __restrict__ npairs_ptr, unsigned long long pair_cap,
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
                 unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
@@ -265,7 +280,8 @@ __global__ void __launch_bounds__(kGramThreads, 1)
 {
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(sm + GramSmem::bars);
+    const GramSmem SL = GramSmem::make(KCH);
+    uint64_t* bars = (uint64_t*)(sm + SL.bars);
     uint64_t* a_full = bars;
     uint64_t* a_empty = bars + 1;
     uint64_t* b_full = bars + 2;
@@ -274,10 +290,10 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     uint64_t* tempty = tfull + kAccBufs;
     uint64_t* drain = tempty + kAccBufs;
     // ring slots: one item (all K-chunks of its B tile) per slot
-    const int nslots = min(kMaxSlots, kRingBytes / (kchunks * kChunkBytes));
-    const uint32_t slot_bytes = (uint32_t)(kchunks * kChunkBytes);
-    uint32_t* tmem_slot = (uint32_t*)(sm + GramSmem::misc);
-    volatile int* abort_flag = (volatile int*)(sm + GramSmem::misc + 4);
+    const int nslots = SL.nslots;
+    const uint32_t slot_bytes = SL.slot_bytes;
+    uint32_t* tmem_slot = (uint32_t*)(sm + SL.misc);
+    volatile int* abort_flag = (volatile int*)(sm + SL.misc + 4);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
@@ -320,27 +336,32 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             bool ok = true;
             PairPrefetch pf;
             pf.init(pairs, wbeg, wend);
-            uint32_t it = 0;
-            for (unsigned long long w = wbeg; ok && w < wend; ++w, ++it) {
+            int q = 0;
+            uint32_t ph = 0;
+            for (unsigned long long w = wbeg; ok && w < wend; ++w) {
                 const int2 tp = pf.next(w);
                 if (tp.x != cur_i) {
                     if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
                     mbar_expect_tx(a_full, slot_bytes);
-                    for (int kc = 0; kc < kchunks; ++kc)
-                        tma_load_2d(sm + GramSmem::a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK,
+#pragma unroll
+                    for (int kc = 0; kc < KCH; ++kc)
+                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK,
                                     tp.x * kTile);
                     ++aloads;
                     cur_i = tp.x;
                 }
-                const int q = (int)(it % (uint32_t)nslots);
-                const uint32_t ph = (it / (uint32_t)nslots) & 1u;
                 if (!mbar_wait_fast(&b_empty[q], ph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
                 mbar_expect_tx(&b_full[q], slot_bytes);
-                uint8_t* slot = sm + GramSmem::b_ring + q * slot_bytes;
-                for (int kc = 0; kc < kchunks; ++kc)
+                uint8_t* slot = sm + SL.b_ring + q * slot_bytes;
+#pragma unroll
+                for (int kc = 0; kc < KCH; ++kc)
                     tma_load_2d(slot + kc * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, tp.y * kTile);
                 issued[q] = true;
                 last_phase[q] = ph;
+                if (++q == nslots) {
+                    q = 0;
+                    ph ^= 1u;
+                }
             }
             if (!ok) {
                 // drain: the copies in flight must land before the CTA exits
@@ -359,12 +380,20 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     } else if (warp == 1) {
         if (lane == 0) {
             // ---------------- MMA issuer
-            uint32_t local = 0, aidx = 0;
+            // One thread issues every MMA, so the loop keeps its scalar work minimal: slot,
+            // accumulator and phases advance incrementally, descriptors step by constants,
+            // and the K loop is unrolled at compile time.
+            uint32_t aidx = 0, ph = 0, tph = 0;
+            int q = 0, b = 0;
             int cur_i = -1;
             bool ok = true, any = false;
+            const uint64_t adesc0 = sw128_desc(smem_u32(sm + SL.a_tile));
+            const uint64_t bdesc_ring = sw128_desc(smem_u32(sm + SL.b_ring));
+            const uint64_t slot_step = (uint64_t)(slot_bytes >> 4);  // descriptor address units
+            uint64_t bdesc_q = bdesc_ring;
             PairPrefetch pf;
             pf.init(pairs, wbeg, wend);
-            for (unsigned long long w = wbeg; ok && w < wend; ++w, ++local) {
+            for (unsigned long long w = wbeg; ok && w < wend; ++w) {
                 const int2 tp = pf.next(w);
                 if (tp.x != cur_i) {
                     if (!mbar_wait_fast(a_full, aidx & 1u, abort_flag, fault, 3)) { ok = false; break; }
@@ -372,29 +401,33 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                     cur_i = tp.x;
                     tc_fence_after();
                 }
-                const int b = (int)(local % kAccBufs);
-                const uint32_t tph = (local / kAccBufs) & 1u;
                 if (!mbar_wait_fast(&tempty[b], tph ^ 1u, abort_flag, fault, 4)) { ok = false; break; }
-                const int q = (int)(local % (uint32_t)nslots);
-                const uint32_t ph = (local / (uint32_t)nslots) & 1u;
                 if (!mbar_wait_fast(&b_full[q], ph, abort_flag, fault, 5)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols);
-                const uint32_t a0 = smem_u32(sm + GramSmem::a_tile);
-                const uint32_t b0 = smem_u32(sm + GramSmem::b_ring + q * slot_bytes);
-                for (int kc = 0; kc < kchunks; ++kc) {
-                    const uint64_t adesc = sw128_desc(a0 + kc * kChunkBytes);
-                    const uint64_t bdesc = sw128_desc(b0 + kc * kChunkBytes);
+#pragma unroll
+                for (int kc = 0; kc < KCH; ++kc)
 #pragma unroll
                     for (int k = 0; k < kChunkK / 16; ++k)
-                        umma_bf16(tacc, adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), kIdesc,
+                        umma_bf16(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
+                                  bdesc_q + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k), kIdesc,
                                   (kc | k) != 0 ? 1u : 0u);
-                }
                 any = true;
                 umma_commit(&b_empty[q]);
                 umma_commit(&tfull[b]);
                 // release the A tile after its last item's MMAs
                 if (pf.q0.x != cur_i) umma_commit(a_empty);  // pf.q0 is item w + 1 (or -1 past the end)
+                if (++q == nslots) {
+                    q = 0;
+                    ph ^= 1u;
+                    bdesc_q = bdesc_ring;
+                } else {
+                    bdesc_q += slot_step;
+                }
+                if (++b == kAccBufs) {
+                    b = 0;
+                    tph ^= 1u;
+                }
             }
             if (!ok && any) {
                 // wait (bounded) for the MMAs already issued before tensor memory is freed
@@ -414,7 +447,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         const int grp = ew / kGroupWarps;              // this group takes items wbeg + grp, + kEpiGroups, ...
         const int sub = warp & 3;                      // TMEM sub-partition this warp may access
         const int cg = (ew % kGroupWarps) >> 2;        // column group: columns [kEpiCols cg, +kEpiCols)
-        float* colu = (float*)(sm + GramSmem::colinfo) + ew * kEpiCols;
+        float* colu = (float*)(sm + SL.colinfo) + ew * kEpiCols;
         const int r = sub * 32 + lane;
         PairPrefetch pf;
         pf.init(pairs, wbeg + grp, wend, kEpiGroups);
@@ -750,6 +783,28 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
+template <class... Args>
+static void launch_gram(int kchunks, int grid, size_t smem, cudaStream_t s, Args... args)
+{
+    switch (kchunks) {
+        case 1: k_gram_bf16<1><<<grid, kGramThreads, smem, s>>>(args...); break;
+        case 2: k_gram_bf16<2><<<grid, kGramThreads, smem, s>>>(args...); break;
+        case 3: k_gram_bf16<3><<<grid, kGramThreads, smem, s>>>(args...); break;
+        default: k_gram_bf16<4><<<grid, kGramThreads, smem, s>>>(args...); break;
+    }
+}
+
+static void set_gram_smem(int kchunks, size_t smem)
+{
+    const int bytes = (int)smem;
+    switch (kchunks) {
+        case 1: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
+        case 2: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
+        case 3: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
+        default: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
+    }
+}
+
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
 {
     cudaStream_t s = c->stream;
@@ -757,12 +812,10 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(c->tmap);
     unsigned long long* cnt = c->counters.as<unsigned long long>() + 5;
     unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
-    const size_t smem = GramSmem::total + 1024;
-    static bool attr_set = false;
-    if (!attr_set) {
-        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
-    }
+    const GramSmem layout = GramSmem::make(kchunks);
+    RNNG_REQUIRE(layout.nslots >= 2, RNNG_ERR_UNSUPPORTED, "BF16 operand tiles too large for shared memory");
+    const size_t smem = layout.total + 1024;
+    set_gram_smem(kchunks, smem);
     const int grid = L.sched_G;
     RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
     const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
@@ -770,10 +823,10 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
-        k_gram_bf16<<<grid, kGramThreads, smem, s>>>(tm, L.pairs, L.d_tile_pairs, L.tile_pairs, kchunks,
-                                                      (const float4*)c->bf16_rowinfo, (const float*)c->bf16_ucol,
-                                                      (const float2*)c->bf16_tileinfo, L.n, c->bf16_eps_p, kappa,
-                                                      c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word); ++c->launches;
+        launch_gram(kchunks, grid, smem, s, tm, L.pairs, L.d_tile_pairs, L.tile_pairs, (const float4*)c->bf16_rowinfo,
+                    (const float*)c->bf16_ucol, (const float2*)c->bf16_tileinfo, L.n, c->bf16_eps_p, kappa,
+                    c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+        ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));
         unsigned long long got = 0;

@@ -88,8 +88,7 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
     prune_covers(c, L);
     RNNG_CUDA(cudaEventRecord(c->ev[4], s));
     if (mode == RNNG_MODE_BF16_RECHECK) {
-        schedule_pairs(c, L, (int)std::max<unsigned long long>(
-                                 1, std::min<unsigned long long>(L.tile_pairs, (unsigned long long)c->num_sms)));
+        schedule_items(c, L, c->num_sms, gram_item_tiles(L.d));
         prepare_bf16(c, L);
     }
     const int64_t m = tiles_with_retry(c, L, mode, E);
@@ -170,7 +169,8 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->super_lo, &c->super_hi, &c->pair_list, &c->super_list, &c->counters, &c->edges_u,
                           &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
                           &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
-                          &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag};
+                          &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
+                          &c->items, &c->items_tmp, &c->sched_tmp};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

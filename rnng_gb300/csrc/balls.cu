@@ -452,12 +452,13 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
     }
 }
 
-// Schedule of the tile pairs for the persistent Gram kernel.  The pairs are sorted by
-// (row tile, column tile) and cut into chunks of kSchedChunk; chunk k goes to CTA k mod G.
-// Every CTA gets the same number of pairs (within one chunk), all CTAs work on
-// neighbouring rows at any moment (their B tiles are shared through L2), and a CTA
-// reloads its resident A tile at most once per chunk.  Each CTA's chunks are stored
-// contiguously, so the kernel reads one range per CTA.
+// Items of the persistent Gram kernel.  The pairs are sorted by (row tile, column
+// tile); inside a row they are grouped nt at a time into items {i, j0, j1} (j1 = -1 for
+// a row's last odd pair or nt = 1).  The items are cut into chunks of kSchedChunk and
+// chunk k goes to CTA k mod G: every CTA gets the same number of items (within one
+// chunk), all CTAs work on neighbouring rows at any moment (their B tiles are shared
+// through L2), and a CTA reloads its resident A tile at most once per chunk.  Each
+// CTA's chunks are stored contiguously, so the kernel reads one range per CTA.
 __global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, uint64_t* __restrict__ keys)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
@@ -466,15 +467,42 @@ __global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, uint6
     }
 }
 
-__global__ void k_schedule_scatter(const uint64_t* __restrict__ keys, int64_t m, int G,
-                                   const unsigned long long* __restrict__ starts, int2* __restrict__ pairs)
+// start[p] = 1 when sorted pair p opens an item: its offset inside its row is a multiple of nt.
+__global__ void k_item_starts(const uint64_t* __restrict__ keys, int64_t m, int nt, int32_t* __restrict__ start)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t row = keys[p] >> 21;
+        int64_t lo = 0, hi = p;  // first pair of this row
+        while (lo < hi) {
+            const int64_t mid = lo + ((hi - lo) >> 1);
+            if ((keys[mid] >> 21) < row) lo = mid + 1;
+            else hi = mid;
+        }
+        start[p] = ((p - lo) % nt) == 0 ? 1 : 0;
+    }
+}
+
+__global__ void k_items(const uint64_t* __restrict__ keys, int64_t m, int nt, const int32_t* __restrict__ start,
+                        const int32_t* __restrict__ off, int4* __restrict__ items)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!start[p]) continue;
         const uint64_t k = keys[p];
+        const int row = (int)(k >> 21);
+        int j1 = -1;
+        if (nt == 2 && p + 1 < m && (int)(keys[p + 1] >> 21) == row) j1 = (int)(keys[p + 1] & 0x1fffff);
+        items[off[p]] = make_int4(row, (int)(k & 0x1fffff), j1, 0);
+    }
+}
+
+__global__ void k_schedule_scatter(const int4* __restrict__ sorted, int64_t m, int G,
+                                   const unsigned long long* __restrict__ starts, int4* __restrict__ items)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
         const int64_t chunk = p / kSchedChunk;
         const int g = (int)(chunk % G);
         const int64_t dest = (int64_t)starts[g] + (chunk / G) * kSchedChunk + p % kSchedChunk;
-        pairs[dest] = make_int2((int)(k >> 21), (int)(k & 0x1fffff));
+        items[dest] = sorted[p];
     }
 }
 
@@ -562,16 +590,52 @@ void prune_covers(rnng_ctx* c, Layout& L)
     L.d_tile_pairs = cnt + 1;
 }
 
-void schedule_pairs(rnng_ctx* c, Layout& L, int G)
+void schedule_items(rnng_ctx* c, Layout& L, int max_ctas, int nt)
 {
     cudaStream_t s = c->stream;
     const int64_t m = (int64_t)L.tile_pairs;
+    L.item_tiles = nt;
+    RNNG_REQUIRE(L.T < (1 << 21), RNNG_ERR_INVALID, "too many tiles for the tile-pair schedule");
+    RNNG_REQUIRE(m < (int64_t(1) << 31), RNNG_ERR_INVALID, "too many tile pairs for the schedule");
+    const int64_t mg = std::max<int64_t>(m, 1);
+    // items in (row, column) order
+    int64_t ni = 0;
+    c->items.reserve(sizeof(int4) * (size_t)mg);
+    c->items_tmp.reserve(sizeof(int4) * (size_t)mg);
+    int4* sorted = c->items_tmp.as<int4>();
+    if (m > 0) {
+        c->aux6.reserve(sizeof(uint64_t) * 2 * (size_t)m);
+        uint64_t* k0 = c->aux6.as<uint64_t>();
+        uint64_t* k1 = k0 + m;
+        c->sched_tmp.reserve(sizeof(int32_t) * 2 * ((size_t)m + 1));
+        int32_t* start = c->sched_tmp.as<int32_t>();
+        int32_t* off = start + m + 1;
+        const unsigned grid =
+            (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
+        k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, k0); ++c->launches;
+        size_t tmp = 0;
+        const int bits = 21 + bits_for_tiles(L.T);
+        RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, bits, s));
+        c->cub_tmp.reserve(tmp);
+        RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, bits, s)); c->launches += cub_sort_kernels(m, bits);
+        k_item_starts<<<grid, 256, 0, s>>>(k1, m, nt, start); ++c->launches;
+        RNNG_CUDA(cudaMemsetAsync(start + m, 0, sizeof(int32_t), s));
+        exclusive_scan_i32(c, start, off, m + 1);
+        int32_t total = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&total, off + m, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        k_items<<<grid, 256, 0, s>>>(k1, m, nt, start, off, sorted); ++c->launches;
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        ni = total;
+    }
+    L.num_items = (unsigned long long)ni;
+    L.items = c->items.as<int4>();
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(ni, (int64_t)max_ctas));
+    L.sched_G = G;
+    // segment of CTA g: its chunks k = g, g + G, ... (all full but the very last chunk)
     c->sched.reserve(sizeof(unsigned long long) * (G + 1));
     unsigned long long* starts = c->sched.as<unsigned long long>();
     L.sched = starts;
-    L.sched_G = G;
-    // segment of CTA g: its chunks k = g, g + G, ... (all full but the very last chunk)
-    const int64_t nchunks = ceil_div(m, kSchedChunk), tail = m % kSchedChunk;
+    const int64_t nchunks = ceil_div(ni, kSchedChunk), tail = ni % kSchedChunk;
     std::vector<unsigned long long> h(G + 1, 0);
     for (int g = 0; g < G; ++g) {
         int64_t size = (nchunks / G + (g < nchunks % G ? 1 : 0)) * kSchedChunk;
@@ -579,22 +643,11 @@ void schedule_pairs(rnng_ctx* c, Layout& L, int G)
         h[g + 1] = h[g] + (unsigned long long)size;
     }
     RNNG_CUDA(cudaMemcpyAsync(starts, h.data(), sizeof(unsigned long long) * (G + 1), cudaMemcpyHostToDevice, s));
-    if (m == 0) {
-        RNNG_CUDA(cudaStreamSynchronize(s));
-        return;
+    if (ni > 0) {
+        const unsigned grid =
+            (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ni, 256), (int64_t)c->num_sms * 8));
+        k_schedule_scatter<<<grid, 256, 0, s>>>(sorted, ni, G, starts, L.items); ++c->launches;
     }
-    RNNG_REQUIRE(L.T < (1 << 21), RNNG_ERR_INVALID, "too many tiles for the tile-pair schedule");
-    c->aux6.reserve(sizeof(uint64_t) * 2 * (size_t)m);
-    uint64_t* k0 = c->aux6.as<uint64_t>();
-    uint64_t* k1 = k0 + m;
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
-    k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, k0); ++c->launches;
-    size_t tmp = 0;
-    const int bits = 21 + bits_for_tiles(L.T);
-    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, bits, s));
-    c->cub_tmp.reserve(tmp);
-    RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, bits, s)); c->launches += cub_sort_kernels(m, bits);
-    k_schedule_scatter<<<grid, 256, 0, s>>>(k1, m, G, starts, L.pairs); ++c->launches;
     RNNG_CUDA(cudaStreamSynchronize(s));  // h lifetime
 }
 

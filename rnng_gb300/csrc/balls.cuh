@@ -14,8 +14,9 @@ void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchil
 void build_covers(rnng_ctx* c, Layout& L);
 // Surviving tile pairs (i <= j) into L.pairs / L.tile_pairs.
 void prune_covers(rnng_ctx* c, Layout& L);
-// Sorts the tile pairs for G persistent CTAs (row tiles i = g mod G per CTA g, then
-// i, then j) and sets L.sched[g] = first pair of CTA g (L.sched[G] = end).
-void schedule_pairs(rnng_ctx* c, Layout& L, int G);
+// Items of the Gram kernel from the tile pairs: pairs sorted by (i, j), consecutive
+// pairs of a row grouped nt at a time, items cut into chunks dealt round-robin to at
+// most max_ctas CTAs; sets L.items, L.num_items, L.item_tiles, L.sched and L.sched_G.
+void schedule_items(rnng_ctx* c, Layout& L, int max_ctas, int nt);
 
 }  // namespace rnng

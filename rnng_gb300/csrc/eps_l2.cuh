@@ -26,7 +26,12 @@ struct Layout {
     unsigned long long super_pairs = 0, tile_pairs = 0;
     int2* pairs = nullptr;        // surviving tile pairs (i <= j)
     unsigned long long* d_tile_pairs = nullptr;  // device copy of tile_pairs
-    unsigned long long* sched = nullptr;          // per-CTA ranges of the pair list (G + 1 entries)
+    // BF16 Gram items: a row tile with item_tiles column tiles {y, z} (z = -1: none), in
+    // the per-CTA order of the schedule; sched holds the G + 1 range starts
+    int4* items = nullptr;
+    unsigned long long num_items = 0;
+    int item_tiles = 1;
+    unsigned long long* sched = nullptr;
     int sched_G = 0;
 };
 
@@ -55,5 +60,7 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
 void prepare_bf16(rnng_ctx* c, Layout& L);
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E);
 bool bf16_supported(int d);
+// Column tiles per Gram item for dimension d (2: N = 256 MMAs, 1: N = 128).
+int gram_item_tiles(int d);
 
 }  // namespace rnng

@@ -55,22 +55,22 @@ constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
 constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared memory per block (227 KB)
 
 // Offsets inside the dynamic shared block (aligned to 1024 bytes in the kernel): the
-// small parts first, then the resident A tile (kchunks chunks) and as many B item slots
-// of kchunks chunks as the rest of the 227 KB holds.  Operand tiles start on 1024-byte
-// boundaries (128-byte swizzle atoms).
+// small parts first, then the resident A tile (kch chunks) and as many B item slots of
+// nt tiles x kch chunks as the rest of the 227 KB holds.  Operand tiles start on
+// 1024-byte boundaries (128-byte swizzle atoms).
 struct GramSmem {
     uint32_t colinfo, bars, misc, a_tile, b_ring, slot_bytes, total;
     int nslots;
     static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1;  // a_full/empty, b_full/empty, tfull/tempty, drain
-    __host__ __device__ static GramSmem make(int kchunks)
+    __host__ __device__ static GramSmem make(int kch, int nt)
     {
         GramSmem g;
         g.colinfo = 0;                                     // kEpiWarps x kEpiCols floats (u_j)
         g.bars = g.colinfo + kEpiWarps * kEpiCols * 4;     // mbarriers
         g.misc = g.bars + nbars * 8;                       // tmem slot, abort flag
         g.a_tile = (g.misc + 16 + 1023) & ~1023u;
-        g.slot_bytes = (uint32_t)kchunks * kChunkBytes;
-        g.b_ring = g.a_tile + g.slot_bytes;
+        g.slot_bytes = (uint32_t)(kch * nt) * kChunkBytes;
+        g.b_ring = g.a_tile + (uint32_t)kch * kChunkBytes;
         const uint32_t room = kSmemLimit - 1024 - g.b_ring;  // 1024: alignment slack of the block base
         g.nslots = (int)(room / g.slot_bytes);
         if (g.nslots > kMaxSlots) g.nslots = kMaxSlots;
@@ -225,22 +225,26 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
     return d;
 }
 
-// Instruction descriptor for kind::f16: D f32, A and B bf16, both K-major, M = N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kAccCols >> 3) << 17) |
-                            ((uint32_t)(kTile >> 4) << 24);
+// Instruction descriptor for kind::f16: D f32, A and B bf16, both K-major, M = 128,
+// N = 128 nt (nt column tiles per MMA).
+__host__ __device__ constexpr uint32_t gram_idesc(int nt)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)((kAccCols * nt) >> 3) << 17) |
+           ((uint32_t)(kTile >> 4) << 24);
+}
 
-// Four-deep register prefetch of the tile-pair list, so that the dependent global
-// load of the next item's indices is issued several items ahead of its use.
-struct PairPrefetch {
-    int2 q0, q1, q2, q3;
-    const int2* __restrict__ p;
+// Four-deep register prefetch of the item list, so that the dependent global load of
+// the next item is issued several items ahead of its use.
+struct ItemPrefetch {
+    int4 q0, q1, q2, q3;
+    const int4* __restrict__ p;
     unsigned long long end;
     unsigned stride;
-    __device__ __forceinline__ int2 ld(unsigned long long w) const { return w < end ? p[w] : make_int2(-1, -1); }
-    __device__ __forceinline__ void init(const int2* __restrict__ pairs, unsigned long long w, unsigned long long e,
+    __device__ __forceinline__ int4 ld(unsigned long long w) const { return w < end ? p[w] : make_int4(-1, -1, -1, -1); }
+    __device__ __forceinline__ void init(const int4* __restrict__ items, unsigned long long w, unsigned long long e,
                                          unsigned step = 1)
     {
-        p = pairs;
+        p = items;
         end = e;
         stride = step;
         q0 = ld(w);
@@ -249,9 +253,9 @@ struct PairPrefetch {
         q3 = ld(w + 3 * step);
     }
     // returns item w (the next item of this sequence) and prefetches item w + 4 * stride
-    __device__ __forceinline__ int2 next(unsigned long long w)
+    __device__ __forceinline__ int4 next(unsigned long long w)
     {
-        const int2 r = q0;
+        const int4 r = q0;
         q0 = q1;
         q1 = q2;
         q2 = q3;
@@ -263,24 +267,29 @@ struct PairPrefetch {
 // ------------------------------------------------------------------------------------------------
 // the Gram kernel
 //
-// CTA g takes its range of the scheduled tile-pair list: the chunks g, g + G, ... of
-// the pairs sorted by (row tile, column tile).  The A tile (rows of i, all K-chunks)
-// stays resident in shared memory while the row lasts, only B tiles stream through
-// the ring, and all CTAs work on neighbouring rows at the same time so that B tiles
-// are shared through L2.
+// An item is one row tile i with NT column tiles {j0, j1} of the tile-pair list (j1 = -1
+// when the row had no second pair): the B slot holds the NT tiles stacked, one
+// 128 x (128 NT) x 16 MMA per K step computes both tile pairs against the resident A
+// tile, and the accumulator (128 NT TMEM columns; 512 / (128 NT) of them in flight)
+// is read by both epilogue groups, one column tile each (NT = 2), or by the two groups
+// on alternate items (NT = 1).  CTA g takes its range of the scheduled item list: the
+// chunks g, g + G, ... of the items sorted by (row tile, column tile), so the A tile
+// stays resident while its row lasts and all CTAs work on neighbouring rows at the
+// same time (B tiles are shared through L2).
 
-template <int KCH>  // K-chunks of 64 dimensions: dp = 64 KCH
+template <int KCH, int NT>  // KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item
 __global__ void __launch_bounds__(kGramThreads, 1)
-    k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int2* __restrict__ pairs,
-                const unsigned long long* __restrict__ npairs_ptr, unsigned long long pair_cap,
+    k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int4* __restrict__ items, unsigned long long nitems,
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
                 unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
                 const unsigned long long* __restrict__ sched, int* __restrict__ fault)
 {
+    constexpr int kAcc = kTmemCols / (kAccCols * NT);  // accumulators in flight
+    constexpr uint32_t kIdesc = gram_idesc(NT);
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
-    const GramSmem SL = GramSmem::make(KCH);
+    const GramSmem SL = GramSmem::make(KCH, NT);
     uint64_t* bars = (uint64_t*)(sm + SL.bars);
     uint64_t* a_full = bars;
     uint64_t* a_empty = bars + 1;
@@ -289,9 +298,10 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     uint64_t* tfull = bars + 2 + 2 * kMaxSlots;
     uint64_t* tempty = tfull + kAccBufs;
     uint64_t* drain = tempty + kAccBufs;
-    // ring slots: one item (all K-chunks of its B tile) per slot
+    // ring slots: one item (all K-chunks of its NT B tiles) per slot
     const int nslots = SL.nslots;
     const uint32_t slot_bytes = SL.slot_bytes;
+    constexpr uint32_t kTileBytes = (uint32_t)KCH * kChunkBytes;  // one operand tile, all chunks
     uint32_t* tmem_slot = (uint32_t*)(sm + SL.misc);
     volatile int* abort_flag = (volatile int*)(sm + SL.misc + 4);
 
@@ -309,7 +319,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         }
         for (int b = 0; b < kAccBufs; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], kGroupWarps);
+            mbar_init(&tempty[b], kGroupWarps * NT);
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -320,9 +330,8 @@ __global__ void __launch_bounds__(kGramThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    const unsigned long long npairs = min(*npairs_ptr, pair_cap);
-    const unsigned long long wbeg = min(npairs, sched[blockIdx.x]);
-    const unsigned long long wend = min(npairs, sched[blockIdx.x + 1]);
+    const unsigned long long wbeg = min(nitems, sched[blockIdx.x]);
+    const unsigned long long wend = min(nitems, sched[blockIdx.x + 1]);
 
     if (warp == 0) {
         if (lane == 0) {
@@ -334,28 +343,33 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             bool issued[kMaxSlots];
             for (int q = 0; q < kMaxSlots; ++q) { issued[q] = false; last_phase[q] = 0; }
             bool ok = true;
-            PairPrefetch pf;
-            pf.init(pairs, wbeg, wend);
+            ItemPrefetch pf;
+            pf.init(items, wbeg, wend);
             int q = 0;
             uint32_t ph = 0;
             for (unsigned long long w = wbeg; ok && w < wend; ++w) {
-                const int2 tp = pf.next(w);
-                if (tp.x != cur_i) {
+                const int4 it = pf.next(w);
+                if (it.x != cur_i) {
                     if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
-                    mbar_expect_tx(a_full, slot_bytes);
+                    mbar_expect_tx(a_full, kTileBytes);
 #pragma unroll
                     for (int kc = 0; kc < KCH; ++kc)
-                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK,
-                                    tp.x * kTile);
+                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK, it.x * kTile);
                     ++aloads;
-                    cur_i = tp.x;
+                    cur_i = it.x;
                 }
                 if (!mbar_wait_fast(&b_empty[q], ph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
-                mbar_expect_tx(&b_full[q], slot_bytes);
+                const bool second = NT == 2 && it.z >= 0;
+                mbar_expect_tx(&b_full[q], second ? 2 * kTileBytes : kTileBytes);
                 uint8_t* slot = sm + SL.b_ring + q * slot_bytes;
+                // chunk kc of tile t at slot + (kc NT + t) 16 KB: per chunk the NT tiles are
+                // stacked rows of one 128 NT-row operand
 #pragma unroll
-                for (int kc = 0; kc < KCH; ++kc)
-                    tma_load_2d(slot + kc * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, tp.y * kTile);
+                for (int kc = 0; kc < KCH; ++kc) {
+                    tma_load_2d(slot + (kc * NT) * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, it.y * kTile);
+                    if (second)
+                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, it.z * kTile);
+                }
                 issued[q] = true;
                 last_phase[q] = ph;
                 if (++q == nslots) {
@@ -369,10 +383,10 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                 if (aloads > 0)
                     while (!mbar_try_wait(a_full, (aloads - 1) & 1u) && globaltimer() - t0 < kWaitNs) {
                     }
-                for (int q = 0; q < kMaxSlots; ++q) {
-                    if (!issued[q]) continue;
+                for (int qq = 0; qq < kMaxSlots; ++qq) {
+                    if (!issued[qq]) continue;
                     t0 = globaltimer();
-                    while (!mbar_try_wait(&b_full[q], last_phase[q]) && globaltimer() - t0 < kWaitNs) {
+                    while (!mbar_try_wait(&b_full[qq], last_phase[qq]) && globaltimer() - t0 < kWaitNs) {
                     }
                 }
             }
@@ -391,26 +405,26 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             const uint64_t bdesc_ring = sw128_desc(smem_u32(sm + SL.b_ring));
             const uint64_t slot_step = (uint64_t)(slot_bytes >> 4);  // descriptor address units
             uint64_t bdesc_q = bdesc_ring;
-            PairPrefetch pf;
-            pf.init(pairs, wbeg, wend);
+            ItemPrefetch pf;
+            pf.init(items, wbeg, wend);
             for (unsigned long long w = wbeg; ok && w < wend; ++w) {
-                const int2 tp = pf.next(w);
-                if (tp.x != cur_i) {
+                const int4 it = pf.next(w);
+                if (it.x != cur_i) {
                     if (!mbar_wait_fast(a_full, aidx & 1u, abort_flag, fault, 3)) { ok = false; break; }
                     ++aidx;
-                    cur_i = tp.x;
+                    cur_i = it.x;
                     tc_fence_after();
                 }
                 if (!mbar_wait_fast(&tempty[b], tph ^ 1u, abort_flag, fault, 4)) { ok = false; break; }
                 if (!mbar_wait_fast(&b_full[q], ph, abort_flag, fault, 5)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols);
+                const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols * NT);
 #pragma unroll
                 for (int kc = 0; kc < KCH; ++kc)
 #pragma unroll
                     for (int k = 0; k < kChunkK / 16; ++k)
                         umma_bf16(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
-                                  bdesc_q + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k), kIdesc,
+                                  bdesc_q + (uint64_t)(kc * NT * (kChunkBytes >> 4) + 2 * k), kIdesc,
                                   (kc | k) != 0 ? 1u : 0u);
                 any = true;
                 umma_commit(&b_empty[q]);
@@ -424,7 +438,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                 } else {
                     bdesc_q += slot_step;
                 }
-                if (++b == kAccBufs) {
+                if (++b == kAcc) {
                     b = 0;
                     tph ^= 1u;
                 }
@@ -443,43 +457,56 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         // and W_i = A_i^2 + q_i - n_i + 2 A_i amax_J (+ rounding slack), A_i = eps' + a_i.
         // Replacing a_j by the column tile's max a only widens the test, so it still
         // admits every pair with (eps' + a_i + a_j)^2 + q_i + q_j >= D~.
+        //
+        // Units: NT = 2: every item, this group's column tile (half = group);
+        //        NT = 1: the items of this group (grp, grp + 2, ...), their only tile.
         const int ew = warp - 2;
-        const int grp = ew / kGroupWarps;              // this group takes items wbeg + grp, + kEpiGroups, ...
+        const int grp = ew / kGroupWarps;
         const int sub = warp & 3;                      // TMEM sub-partition this warp may access
         const int cg = (ew % kGroupWarps) >> 2;        // column group: columns [kEpiCols cg, +kEpiCols)
+        const int half = NT == 2 ? grp : 0;
+        const unsigned ustride = NT == 2 ? 1u : (unsigned)kEpiGroups;
+        const unsigned long long ubeg = wbeg + (NT == 2 ? 0 : grp);
         float* colu = (float*)(sm + SL.colinfo) + ew * kEpiCols;
         const int r = sub * 32 + lane;
-        PairPrefetch pf;
-        pf.init(pairs, wbeg + grp, wend, kEpiGroups);
-        // row / column data of the current item, loaded one item ahead
-        int2 tp = pf.next(wbeg + grp);
+        ItemPrefetch pf;
+        pf.init(items, ubeg, wend, ustride);
+        // row / column data of the current unit, loaded one unit ahead
+        int4 it = pf.next(ubeg);
         float2 uc = make_float2(0.f, 0.f);
         float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
         float2 tj = make_float2(0.f, 0.f);
-        if (wbeg + grp < wend) {
-            uc = reinterpret_cast<const float2*>(ucol)[((int64_t)tp.y * kTile + cg * kEpiCols) / 2 + lane];
-            ri = rowinfo[(int64_t)tp.x * kTile + r];
-            tj = tileinfo[tp.y];
+        {
+            const int jt = half ? it.z : it.y;
+            if (ubeg < wend && jt >= 0) {
+                uc = reinterpret_cast<const float2*>(ucol)[((int64_t)jt * kTile + cg * kEpiCols) / 2 + lane];
+                ri = rowinfo[(int64_t)it.x * kTile + r];
+                tj = tileinfo[jt];
+            }
         }
-        uint32_t local = (uint32_t)grp;
-        for (unsigned long long w = wbeg + grp; w < wend; w += kEpiGroups, local += kEpiGroups) {
-            const int b = (int)(local % kAccBufs);
-            const uint32_t tph = (local / kAccBufs) & 1u;
-            const int64_t j0 = (int64_t)tp.y * kTile + cg * kEpiCols;
-            const int64_t gi = (int64_t)tp.x * kTile + r;
-            const bool diag = tp.x == tp.y;
+        uint32_t local = (uint32_t)(ubeg - wbeg);  // item index within the CTA's range
+        for (unsigned long long w = ubeg; w < wend; w += ustride, local += ustride) {
+            const int b = (int)(local % (uint32_t)kAcc);
+            const uint32_t tph = (local / (uint32_t)kAcc) & 1u;
+            const int jt = half ? it.z : it.y;  // this unit's column tile (-1: none)
+            const int64_t j0 = (int64_t)jt * kTile + cg * kEpiCols;
+            const int64_t gi = (int64_t)it.x * kTile + r;
+            const bool diag = it.x == jt;
             reinterpret_cast<float2*>(colu)[lane] = uc;
             const float A = eps_p + ri.y;
             const float AA = A * A, cross = 2.f * A * tj.x;
             const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
-            // issue the next item's loads now; they complete while this item is tested
-            const int2 tpn = pf.next(w + kEpiGroups);
-            if (w + kEpiGroups < wend) {
-                uc = reinterpret_cast<const float2*>(ucol)[((int64_t)tpn.y * kTile + cg * kEpiCols) / 2 + lane];
-                ri = rowinfo[(int64_t)tpn.x * kTile + r];
-                tj = tileinfo[tpn.y];
+            // issue the next unit's loads now; they complete while this one is tested
+            const int4 itn = pf.next(w + ustride);
+            {
+                const int jn = half ? itn.z : itn.y;
+                if (w + ustride < wend && jn >= 0) {
+                    uc = reinterpret_cast<const float2*>(ucol)[((int64_t)jn * kTile + cg * kEpiCols) / 2 + lane];
+                    ri = rowinfo[(int64_t)itn.x * kTile + r];
+                    tj = tileinfo[jn];
+                }
             }
-            tp = tpn;
+            it = itn;
             __syncwarp();
             // fast path: the accumulator is usually ready; otherwise lane 0 waits (bounded)
             if (!__all_sync(0xffffffffu, mbar_try_wait(&tfull[b], tph))) {
@@ -490,7 +517,15 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                 }
             }
             tc_fence_after();
-            const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) + (uint32_t)(b * kAccCols + cg * kEpiCols);
+            if (jt < 0) {
+                // no second tile in this item: nothing to test, hand the accumulator back
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&tempty[b]);
+                continue;
+            }
+            const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) +
+                                   (uint32_t)(b * kAccCols * NT + half * kAccCols + cg * kEpiCols);
             for (int ch = 0; ch < kEpiCols / 32; ++ch) {
                 float g[32];
                 tmem_ld32(taddr + ch * 32, g);
@@ -783,26 +818,41 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <class... Args>
-static void launch_gram(int kchunks, int grid, size_t smem, cudaStream_t s, Args... args)
+template <int KCH, int NT>
+static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, const CUtensorMap& tm, const int4* items,
+                          unsigned long long nitems, const float4* rowinfo, const float* ucol, const float2* tileinfo,
+                          int64_t n, float eps_p, float kappa, uint2* cand, unsigned long long* cnt,
+                          unsigned long long ccap, const unsigned long long* sched, int* fault)
 {
-    switch (kchunks) {
-        case 1: k_gram_bf16<1><<<grid, kGramThreads, smem, s>>>(args...); break;
-        case 2: k_gram_bf16<2><<<grid, kGramThreads, smem, s>>>(args...); break;
-        case 3: k_gram_bf16<3><<<grid, kGramThreads, smem, s>>>(args...); break;
-        default: k_gram_bf16<4><<<grid, kGramThreads, smem, s>>>(args...); break;
+    if (!launch) {
+        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return;
+    }
+    k_gram_bf16<KCH, NT><<<grid, kGramThreads, smem, s>>>(tm, items, nitems, rowinfo, ucol, tileinfo, n, eps_p, kappa,
+                                                          cand, cnt, ccap, sched, fault);
+}
+
+// Sets the shared-memory size (launch = false) or launches the instance for (kch, nt).
+template <class... Args>
+static void gram_dispatch(int kch, int nt, Args... args)
+{
+    if (nt == 2) {
+        if (kch == 1) gram_instance<1, 2>(args...);
+        else gram_instance<2, 2>(args...);
+    } else {
+        switch (kch) {
+            case 1: gram_instance<1, 1>(args...); break;
+            case 2: gram_instance<2, 1>(args...); break;
+            case 3: gram_instance<3, 1>(args...); break;
+            default: gram_instance<4, 1>(args...); break;
+        }
     }
 }
 
-static void set_gram_smem(int kchunks, size_t smem)
+int gram_item_tiles(int d)
 {
-    const int bytes = (int)smem;
-    switch (kchunks) {
-        case 1: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
-        case 2: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
-        case 3: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
-        default: RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)); break;
-    }
+    // two column tiles per item (N = 256 MMAs) while two B slots of them fit next to A
+    return ceil_div(d, kChunkK) <= 2 ? 2 : 1;
 }
 
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
@@ -812,10 +862,15 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(c->tmap);
     unsigned long long* cnt = c->counters.as<unsigned long long>() + 5;
     unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
-    const GramSmem layout = GramSmem::make(kchunks);
+    const int nt = L.item_tiles;
+    const GramSmem layout = GramSmem::make(kchunks, nt);
     RNNG_REQUIRE(layout.nslots >= 2, RNNG_ERR_UNSUPPORTED, "BF16 operand tiles too large for shared memory");
     const size_t smem = layout.total + 1024;
-    set_gram_smem(kchunks, smem);
+    const float4* rowinfo = (const float4*)c->bf16_rowinfo;
+    const float* ucol = (const float*)c->bf16_ucol;
+    const float2* tileinfo = (const float2*)c->bf16_tileinfo;
+    gram_dispatch(kchunks, nt, false, 0, smem, s, tm, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n, c->bf16_eps_p,
+                  0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
     const int grid = L.sched_G;
     RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
     const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
@@ -823,9 +878,8 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
-        launch_gram(kchunks, grid, smem, s, tm, L.pairs, L.d_tile_pairs, L.tile_pairs, (const float4*)c->bf16_rowinfo,
-                    (const float*)c->bf16_ucol, (const float2*)c->bf16_tileinfo, L.n, c->bf16_eps_p, kappa,
-                    c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+        gram_dispatch(kchunks, nt, true, grid, smem, s, tm, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n,
+                      c->bf16_eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
         ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));

@@ -377,12 +377,15 @@ __global__ void k_bitmap_pairs(const uint32_t* __restrict__ bitmap, int64_t S, i
     }
 }
 
-// Level 2: one block per surviving super pair.  The two super-tiles' tile balls
-// (kSuper * kBalls each) are staged in shared memory 64 dimensions at a time; each
-// thread accumulates 4 of the 32 x 32 ball-pair distances; a tile pair survives
-// when any of its kBalls x kBalls ball pairs is close.
+// Level 2: 64 threads per surviving super pair, four super pairs per block.  Thread
+// (ti, tj) owns tile pair (ta0 + ti, tb0 + tj) and its kBalls x kBalls ball pairs; the
+// two super-tiles' ball centres are staged in shared memory kDC dimensions at a time,
+// transposed so that one float4 load feeds four balls.  A tile pair survives when any
+// of its ball pairs is close; each distance is the sequential fmaf sum over the
+// dimensions, as at the super level.
 constexpr int kNB = kSuper * kBalls;  // balls per super-tile
-constexpr int kDC = 64;               // dimensions per staged chunk
+constexpr int kDC = 32;               // dimensions per staged chunk
+constexpr int kSPB = 4;               // super pairs per block
 
 __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ supers,
                                                     const unsigned long long* __restrict__ nsup_ptr,
@@ -391,63 +394,95 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
                                                     float shrink, int2* __restrict__ out,
                                                     unsigned long long* __restrict__ count, unsigned long long cap)
 {
-    __shared__ float ca[kNB][kDC + 1], cb[kNB][kDC + 1];
-    __shared__ float ra[kNB], rb[kNB];
-    __shared__ int close_tile[kSuper][kSuper];
+    __shared__ __align__(16) float ca[kSPB][kDC][kNB + 4], cb[kSPB][kDC][kNB + 4];
     const unsigned long long nsup = min(*nsup_ptr, sup_cap);
-    for (unsigned long long w = blockIdx.x; w < nsup; w += gridDim.x) {
-        const int2 sp = supers[w];
-        const int64_t ta0 = (int64_t)sp.x * kSuper, tb0 = (int64_t)sp.y * kSuper;
-        for (int k = threadIdx.x; k < kNB; k += blockDim.x) {
-            const int64_t t1 = ta0 + k / kBalls, t2 = tb0 + k / kBalls;
-            ra[k] = t1 < T ? trad[t1 * kBalls + k % kBalls] : -1.f;
-            rb[k] = t2 < T ? trad[t2 * kBalls + k % kBalls] : -1.f;
-        }
-        for (int k = threadIdx.x; k < kSuper * kSuper; k += blockDim.x) close_tile[k / kSuper][k % kSuper] = 0;
-        // 2 x 2 ball pairs per thread: rows {ti, ti + 16}, columns {tj, tj + 16}
-        const int ti = threadIdx.x >> 4, tj = threadIdx.x & 15;
-        float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    const int sp = threadIdx.x >> 6;       // super pair of this block's four
+    const int t = threadIdx.x & 63;
+    const int ti = t >> 3, tj = t & 7;     // tile pair inside the super pair
+    for (unsigned long long w0 = (unsigned long long)blockIdx.x * kSPB; w0 < nsup;
+         w0 += (unsigned long long)gridDim.x * kSPB) {
+        const unsigned long long w = w0 + sp;
+        const bool live = w < nsup;
+        const int2 spair = live ? supers[w] : make_int2(0, 0);
+        const int64_t ta0 = (int64_t)spair.x * kSuper, tb0 = (int64_t)spair.y * kSuper;
+        float acc[kBalls][kBalls];
+#pragma unroll
+        for (int x = 0; x < kBalls; ++x)
+#pragma unroll
+            for (int y = 0; y < kBalls; ++y) acc[x][y] = 0.f;
         for (int k0 = 0; k0 < d; k0 += kDC) {
             __syncthreads();
-            for (int idx = threadIdx.x; idx < kNB * kDC; idx += blockDim.x) {
-                const int b = idx / kDC, k = k0 + idx % kDC;
-                const int64_t t1 = ta0 + b / kBalls, t2 = tb0 + b / kBalls;
-                ca[b][idx % kDC] = (t1 < T && k < d) ? tcen[(t1 * kBalls + b % kBalls) * (int64_t)d + k] : 0.f;
-                cb[b][idx % kDC] = (t2 < T && k < d) ? tcen[(t2 * kBalls + b % kBalls) * (int64_t)d + k] : 0.f;
+            // stage: kNB balls x kDC dims per side as float4 along the dimension
+            for (int idx = t; idx < kNB * (kDC / 4); idx += 64) {
+                const int ball = idx / (kDC / 4), q4 = idx % (kDC / 4), k = k0 + 4 * q4;
+                const int64_t t1 = ta0 + ball / kBalls, t2 = tb0 + ball / kBalls;
+                float4 va = make_float4(0.f, 0.f, 0.f, 0.f), vb = va;
+                if (live && t1 < T) {
+                    const float* src = tcen + (t1 * kBalls + ball % kBalls) * (int64_t)d;
+                    if (k + 3 < d && (d & 3) == 0) va = *reinterpret_cast<const float4*>(src + k);
+                    else {
+                        va.x = k < d ? src[k] : 0.f;
+                        va.y = k + 1 < d ? src[k + 1] : 0.f;
+                        va.z = k + 2 < d ? src[k + 2] : 0.f;
+                        va.w = k + 3 < d ? src[k + 3] : 0.f;
+                    }
+                }
+                if (live && t2 < T) {
+                    const float* src = tcen + (t2 * kBalls + ball % kBalls) * (int64_t)d;
+                    if (k + 3 < d && (d & 3) == 0) vb = *reinterpret_cast<const float4*>(src + k);
+                    else {
+                        vb.x = k < d ? src[k] : 0.f;
+                        vb.y = k + 1 < d ? src[k + 1] : 0.f;
+                        vb.z = k + 2 < d ? src[k + 2] : 0.f;
+                        vb.w = k + 3 < d ? src[k + 3] : 0.f;
+                    }
+                }
+                ca[sp][4 * q4 + 0][ball] = va.x;
+                ca[sp][4 * q4 + 1][ball] = va.y;
+                ca[sp][4 * q4 + 2][ball] = va.z;
+                ca[sp][4 * q4 + 3][ball] = va.w;
+                cb[sp][4 * q4 + 0][ball] = vb.x;
+                cb[sp][4 * q4 + 1][ball] = vb.y;
+                cb[sp][4 * q4 + 2][ball] = vb.z;
+                cb[sp][4 * q4 + 3][ball] = vb.w;
             }
             __syncthreads();
-#pragma unroll 8
-            for (int k = 0; k < kDC; ++k) {
-                const float a0 = ca[ti][k], a1 = ca[ti + 16][k], b0 = cb[tj][k], b1 = cb[tj + 16][k];
-                const float t00 = a0 - b0, t01 = a0 - b1, t10 = a1 - b0, t11 = a1 - b1;
-                acc[0][0] = fmaf(t00, t00, acc[0][0]);
-                acc[0][1] = fmaf(t01, t01, acc[0][1]);
-                acc[1][0] = fmaf(t10, t10, acc[1][0]);
-                acc[1][1] = fmaf(t11, t11, acc[1][1]);
+            const int kk_end = min(kDC, d - k0);
+#pragma unroll 4
+            for (int kk = 0; kk < kk_end; ++kk) {
+                const float4 a4 = *reinterpret_cast<const float4*>(&ca[sp][kk][ti * kBalls]);
+                const float4 b4 = *reinterpret_cast<const float4*>(&cb[sp][kk][tj * kBalls]);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+                for (int x = 0; x < kBalls; ++x)
+#pragma unroll
+                    for (int y = 0; y < kBalls; ++y) {
+                        const float df = av[x] - bv[y];
+                        acc[x][y] = fmaf(df, df, acc[x][y]);
+                    }
             }
         }
+        const int64_t i = ta0 + ti, j = tb0 + tj;
+        bool keep = false;
+        if (live && i < T && j < T && i <= j) {
 #pragma unroll
-        for (int x = 0; x < 2; ++x)
+            for (int x = 0; x < kBalls; ++x) {
+                const float ra = trad[i * kBalls + x];
 #pragma unroll
-            for (int y = 0; y < 2; ++y) {
-                const int i = ti + 16 * x, j = tj + 16 * y;
-                if (ra[i] >= 0.f && rb[j] >= 0.f && sqrtf(acc[x][y]) * shrink <= eps_p + ra[i] + rb[j])
-                    close_tile[i / kBalls][j / kBalls] = 1;
+                for (int y = 0; y < kBalls; ++y) {
+                    const float rb = trad[j * kBalls + y];
+                    if (ra >= 0.f && rb >= 0.f && sqrtf(acc[x][y]) * shrink <= eps_p + ra + rb) keep = true;
+                }
             }
-        __syncthreads();
-        if (threadIdx.x < kSuper * kSuper) {
-            const int qi = threadIdx.x / kSuper, qj = threadIdx.x % kSuper;
-            const int64_t i = ta0 + qi, j = tb0 + qj;
-            const bool keep = close_tile[qi][qj] && i < T && j < T && i <= j;
-            const unsigned ball = __ballot_sync(0xffffffffu, keep);
-            const int lane = threadIdx.x & 31;
-            unsigned long long base = 0;
-            if (lane == 0 && ball) base = atomicAdd(count, (unsigned long long)__popc(ball));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (keep) {
-                const unsigned long long pos = base + __popc(ball & ((1u << lane) - 1u));
-                if (pos < cap) out[pos] = make_int2((int)i, (int)j);
-            }
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, keep);
+        const int lane = threadIdx.x & 31;
+        unsigned long long base = 0;
+        if (lane == 0 && ball) base = atomicAdd(count, (unsigned long long)__popc(ball));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (keep) {
+            const unsigned long long pos = base + __popc(ball & ((1u << lane) - 1u));
+            if (pos < cap) out[pos] = make_int2((int)i, (int)j);
         }
     }
 }
@@ -578,7 +613,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
     c->pair_list.reserve(sizeof(int2) * tile_cap);
     RNNG_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), s));
     const unsigned grid = (unsigned)std::max<unsigned long long>(
-        1, std::min<unsigned long long>(L.super_pairs, (unsigned long long)c->num_sms * 16));
+        1, std::min<unsigned long long>((L.super_pairs + kSPB - 1) / kSPB, (unsigned long long)c->num_sms * 8));
     k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
                                       c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(), cnt + 1,
                                       tile_cap); ++c->launches;

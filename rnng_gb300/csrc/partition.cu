@@ -47,6 +47,11 @@ __global__ void __launch_bounds__(256) k_assign(const float* __restrict__ X, con
     }
     float best[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
     int bidx[4] = {0, 0, 0, 0};
+    // blocks whose rows all sit in cells that do not split keep their keys: no distances
+    int need = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) need |= (rhi[r] - rlo[r] > 1) ? 1 : 0;
+    if (!__syncthreads_or(need)) hi = lo;
     for (int64_t c0 = lo; c0 < hi; c0 += kDCols) {
         float acc[4][4];
         dist_block(sm, X, rowmap, r0, nrows, d, C, c0, hi, acc);

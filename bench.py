@@ -157,6 +157,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="points of the descriptor workload (smaller sizes are for ncu captures only)")
+    ap.add_argument("--workload", default="k2", choices=["k1", "k2", "k3", "k4", "k5"],
+                    help="k2 (default) is the headline; k1, k3, k4, k5 print the same line for the other "
+                         "configurations (see SECONDARY)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -166,6 +169,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload != "k2":
+        run_secondary(args, world, rank, local)
         return
 
     import torch
@@ -285,6 +291,151 @@ def main():
                                                 "ms_finalize")}}, n),
                 "fp32_direct": fp32, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "gpu_launches": int(sum(launches)), "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    ctx.close()
+
+
+# ----------------------------------------------------------------------------- other configurations
+
+SECONDARY = {
+    "k1": {"metric": "eps-graph edges/s, 20k x 8 f32 Gaussian mixture, eps 1.5", "unit": "edges/s"},
+    "k3": {"metric": "eps-graph edges/s, 200k DNA strings, edit distance, eps 8", "unit": "edges/s"},
+    "k4": {"metric": "Rips filtration simplices/s (<= 2-simplices), 500k torus points in R^16", "unit": "simplices/s"},
+    "k5": {"metric": "eps-graph edges/s, 5M x 32 f32 Zipf Gaussian mixture", "unit": "edges/s"},
+}
+
+
+def run_secondary(args, world, rank, local):
+    """K1, K3, K4, K5: one call of the path per step on device-resident input (value) and
+    from host buffers (e2e), timed like the headline line."""
+    import torch
+    import rnng_gb300
+    from rnng_gb300 import synth
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    ctx = rnng_gb300.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=f"cuda:{local}")
+    dev = f"cuda:{local}"
+    flags_dev = rnng_gb300.INPUT_DEVICE | rnng_gb300.OUTPUT_DEVICE
+    wl = args.workload
+    cfg = {}
+    if wl in ("k1", "k5"):
+        x = synth.l2_mixture() if wl == "k1" else synth.zipf_mixture()
+        radius = synth.EPS_K1 if wl == "k1" else synth.EPS_K5
+        n, d = x.shape
+        xd = torch.from_numpy(x).to(dev)
+        xh = torch.from_numpy(x).pin_memory()
+        cfg = {"workload": {"k1": "k1-gaussian-mixture-20kx8-f32", "k5": "k5-zipf-mixture-5Mx32-f32"}[wl],
+               "points": n, "dim": d, "radius": float(radius)}
+        step = lambda mode=1: ctx.eps_graph_l2_raw(xd.data_ptr(), None, n, d, radius, mode, flags_dev).count
+        step_host = lambda: ctx.eps_graph_l2_raw(xh.data_ptr(), None, n, d, radius, 1, 0).count
+        h2d = n * d * 4
+        d2h_per_unit = 8 + 8 + 4
+    elif wl == "k3":
+        seqs = synth.dna_families()
+        atoms, offsets = synth.pack_seqs(seqs)
+        radius = synth.EPS_K3
+        n = offsets.size - 1
+        ad, od = torch.from_numpy(atoms).to(dev), torch.from_numpy(offsets).to(dev)
+        ah, oh = torch.from_numpy(atoms).pin_memory(), torch.from_numpy(offsets).pin_memory()
+        cfg = {"workload": "k3-dna-families-200k-edit", "strings": n, "atoms": int(atoms.size),
+               "radius": float(radius)}
+        step = lambda mode=1: ctx.eps_graph_edit_raw(ad.data_ptr(), od.data_ptr(), n, radius, flags_dev).count
+        step_host = lambda: ctx.eps_graph_edit_raw(ah.data_ptr(), oh.data_ptr(), n, radius, 0).count
+        h2d = int(atoms.size + offsets.size * 8)
+        d2h_per_unit = 8 + 8 + 4
+    else:  # k4
+        x = synth.torus16()
+        radius = synth.EPS_K4
+        n, d = x.shape
+        xd = torch.from_numpy(x).to(dev)
+        xh = torch.from_numpy(x).pin_memory()
+        cfg = {"workload": "k4-torus16-500k-rips-maxdim2", "points": n, "dim": d, "radius": float(radius),
+               "maxdim": 2}
+        step = lambda mode=1: ctx.rips_l2_raw(xd.data_ptr(), n, d, radius, 2, mode, flags_dev).count
+        step_host = lambda: ctx.rips_l2_raw(xh.data_ptr(), n, d, radius, 2, 1, 0).count
+        h2d = n * d * 4
+        d2h_per_unit = 8 + 4
+    for _ in range(args.warmup):
+        units = step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches, stats = [], []
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        units = step()
+        st = ctx.stats()
+        launches.append(st["kernel_launches"])
+        stats.append(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * units * args.steps / (ms / 1e3)
+    last = stats[-1]
+    fp32 = None
+    if wl in ("k1", "k5", "k4") and args.fp32_steps > 0:
+        step(0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.fp32_steps):
+            u32 = step(0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = e0.elapsed_time(e1) / args.fp32_steps
+        assert u32 == units, "FP32 and BF16 forms differ"
+        fp32 = {"value": units / (ms32 / 1e3), "ms_per_step": ms32, "bf16_speedup": ms32 / (ms / args.steps)}
+    step_host()
+    t_e2e = []
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = step_host()
+        t_e2e.append(time.perf_counter() - t0)
+        assert u == units
+    e2e_s = statistics.median(t_e2e)
+    roofline = None
+    if wl in ("k1", "k5") and last["ms_gram"] > 0:
+        peak = 1900.0
+        src = "of fallback"
+        try:
+            peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops_sustained"])
+            src = "of measured (sustained bf16)"
+        except (OSError, KeyError, ValueError):
+            pass
+        dp = -(-d // 64) * 64
+        flops = 2.0 * dp * last["pairs_evaluated"]
+        achieved = flops / (statistics.median(s["ms_gram"] for s in stats) / 1e3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "k_gram_bf16", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "peak_source": src, "traffic": None,
+                    "algorithmic": "2*dp flops per evaluated pair (dp = d padded to 64)"}
+    if rank == 0:
+        cfg.update({"units": int(units), "parallelism": "replicas" if world > 1 else "single-gpu",
+                    "stage_ms": {k: round(last[k], 3) for k in ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles",
+                                                                "ms_recheck", "ms_finalize", "ms_total")},
+                    "tile_pairs": int(last["tile_pairs"]), "candidates": int(last["candidates"])})
+        line = {"metric": SECONDARY[wl]["metric"], "value": value, "unit": SECONDARY[wl]["unit"], "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl == "k3" else "bf16",
+                "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)", "config": cfg, "fp32_direct": fp32,
+                "e2e": {"value": world * units / e2e_s, "unit": SECONDARY[wl]["unit"], "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(units * d2h_per_unit), "ms_per_step": e2e_s * 1e3},
+                "roofline": roofline, "cpu_baseline": None, "gpu_launches": int(sum(launches)), "clocks": clk}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

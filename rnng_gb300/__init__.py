@@ -213,6 +213,22 @@ class Context:
         self._check(rc, self.h)
         return e
 
+    def eps_graph_edit_raw(self, atoms_ptr: int, offsets_ptr: int, n: int, radius, flags: int) -> Edges:
+        """Direct C-ABI call with raw pointers (benchmark use)."""
+        e = Edges()
+        rc = self.lib.rnng_eps_graph_edit(self.h, atoms_ptr, offsets_ptr, None, n, ctypes.c_float(radius), flags,
+                                          ctypes.byref(e))
+        self._check(rc, self.h)
+        return e
+
+    def rips_l2_raw(self, x_ptr: int, n: int, d: int, radius, maxdim: int, mode: int, flags: int) -> Simplices:
+        """Direct C-ABI call with raw pointers (benchmark use)."""
+        s = Simplices()
+        rc = self.lib.rnng_rips_l2(self.h, x_ptr, None, n, d, ctypes.c_float(radius), maxdim, mode, flags,
+                                   ctypes.byref(s))
+        self._check(rc, self.h)
+        return s
+
     def radius_query_l2(self, X, Q, radius, ids=None, qids=None, sort: bool = True):
         X = np.ascontiguousarray(X, dtype=np.float32)
         Q = np.ascontiguousarray(Q, dtype=np.float32)

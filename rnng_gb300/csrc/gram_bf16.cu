@@ -536,15 +536,17 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                     if (lane == 0) mbar_arrive(&tempty[b]);
                 }
                 // most rows have no candidate: test the minimum first
-                float mn = INFINITY;
+                // four independent running minima keep the dependent chain short
+                float m0 = INFINITY, m1 = INFINITY, m2 = INFINITY, m3 = INFINITY;
 #pragma unroll
                 for (int t4 = 0; t4 < 8; ++t4) {
                     const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
-                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 0], u4.x));
-                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 1], u4.y));
-                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 2], u4.z));
-                    mn = fminf(mn, fmaf(-2.f, g[4 * t4 + 3], u4.w));
+                    m0 = fminf(m0, fmaf(-2.f, g[4 * t4 + 0], u4.x));
+                    m1 = fminf(m1, fmaf(-2.f, g[4 * t4 + 1], u4.y));
+                    m2 = fminf(m2, fmaf(-2.f, g[4 * t4 + 2], u4.z));
+                    m3 = fminf(m3, fmaf(-2.f, g[4 * t4 + 3], u4.w));
                 }
+                const float mn = fminf(fminf(m0, m1), fminf(m2, m3));
                 const bool mine = mn <= Wi;
                 if (!__any_sync(0xffffffffu, mine)) continue;
                 uint32_t m = 0;

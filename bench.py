@@ -144,6 +144,22 @@ def cpu_value(leg: dict, edges: int, n: int) -> float:
     return edges / (leg["pair_time_s"] * n * (n - 1) / 2)
 
 
+def max_over_ranks(ms: float, dist, device) -> float:
+    """The slowest rank's time: every replica does the full workload, the job's time is
+    the maximum (dist is torch.distributed or None for one process)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: int, world: int, steps: int, ms: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * units_per_rank * steps / (ms / 1e3)
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -215,13 +231,9 @@ def main():
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, f"cuda:{local}")
     ms_step = ms / args.steps
-    value = world * edges * args.steps / (ms / 1e3)
+    value = job_value(edges, world, args.steps, ms)
     last = ctx.stats()
 
     # ---- plain FP32 form (same partition and pruning), a few steps
@@ -380,12 +392,8 @@ def run_secondary(args, world, rank, local):
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * units * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
+    value = job_value(units, world, args.steps, ms)
     last = stats[-1]
     fp32 = None
     if wl in ("k1", "k5", "k4") and args.fp32_steps > 0:

@@ -100,14 +100,18 @@ __global__ void k_edit_emit_pairs(const int32_t* __restrict__ cnt, const int32_t
 }
 
 // Filter: length and profile L1 tests for all pairs of each tile pair; survivors are
-// appended as (sorted index a, sorted index b), a < b.
+// appended as (sorted index a, sorted index b), a < b.  The profile L1 sums are a small
+// integer GEMM: thread (ty, tx) keeps the 8 x 8 block of rows ty*8.. and columns tx*8..,
+// and for every profile word loads 8 words of each side (two 16-byte loads per side from
+// the word-major shared copy) for 64 __vsadu4; the length test masks the block afterwards.
 __global__ void __launch_bounds__(256) k_edit_filter(const uint32_t* __restrict__ prof,
                                                      const uint32_t* __restrict__ slen, int64_t n,
                                                      const int2* __restrict__ pairs, int64_t npairs, int K,
                                                      uint2* __restrict__ cand, unsigned long long* __restrict__ ccount,
                                                      unsigned long long cap)
 {
-    __shared__ uint32_t pa[kET][kBins / 4 + 1], pb[kET][kBins / 4 + 1];
+    constexpr int kW = kBins / 4;  // profile words per string
+    __shared__ __align__(16) uint32_t pa[kW][kET], pb[kW][kET];
     __shared__ uint32_t la[kET], lb[kET];
     __shared__ int s_warp[8];
     __shared__ unsigned long long s_base;
@@ -117,16 +121,43 @@ __global__ void __launch_bounds__(256) k_edit_filter(const uint32_t* __restrict_
         const int2 tp = pairs[w];
         const int64_t i0 = (int64_t)tp.x * kET, j0 = (int64_t)tp.y * kET;
         __syncthreads();
-        for (int idx = tid; idx < kET * (kBins / 4); idx += 256) {
-            const int r = idx / (kBins / 4), k = idx % (kBins / 4);
-            pa[r][k] = prof[(i0 + r) * (kBins / 4) + k];
-            pb[r][k] = prof[(j0 + r) * (kBins / 4) + k];
+        // coalesced 16-byte loads of four profile words, stored word-major
+        for (int idx = tid; idx < kET * (kW / 4); idx += 256) {
+            const int r = idx / (kW / 4), q = idx % (kW / 4);
+            const uint4 va = reinterpret_cast<const uint4*>(prof)[(i0 + r) * (kW / 4) + q];
+            const uint4 vb = reinterpret_cast<const uint4*>(prof)[(j0 + r) * (kW / 4) + q];
+            pa[4 * q + 0][r] = va.x;
+            pa[4 * q + 1][r] = va.y;
+            pa[4 * q + 2][r] = va.z;
+            pa[4 * q + 3][r] = va.w;
+            pb[4 * q + 0][r] = vb.x;
+            pb[4 * q + 1][r] = vb.y;
+            pb[4 * q + 2][r] = vb.z;
+            pb[4 * q + 3][r] = vb.w;
         }
         for (int r = tid; r < kET; r += 256) {
             la[r] = i0 + r < n ? slen[i0 + r] : 0xffffffffu;
             lb[r] = j0 + r < n ? slen[j0 + r] : 0xffffffffu;
         }
         __syncthreads();
+        uint32_t l1s[8][8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) l1s[r][c] = 0;
+#pragma unroll 2
+        for (int k = 0; k < kW; ++k) {
+            const uint4 a0 = *reinterpret_cast<const uint4*>(&pa[k][ty * 8]);
+            const uint4 a1 = *reinterpret_cast<const uint4*>(&pa[k][ty * 8 + 4]);
+            const uint4 b0 = *reinterpret_cast<const uint4*>(&pb[k][tx * 8]);
+            const uint4 b1 = *reinterpret_cast<const uint4*>(&pb[k][tx * 8 + 4]);
+            const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const uint32_t bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) l1s[r][c] = __vsadu4(av[r], bv[c]) + l1s[r][c];
+        }
         uint64_t mask = 0;  // 8 x 8 block of this thread
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
@@ -137,14 +168,8 @@ __global__ void __launch_bounds__(256) k_edit_filter(const uint32_t* __restrict_
                 const int cb = tx * 8 + c;
                 const uint32_t l2 = lb[cb];
                 const uint32_t dl = l1 > l2 ? l1 - l2 : l2 - l1;
-                bool ok = (l1 != 0xffffffffu) && (l2 != 0xffffffffu) && dl <= (uint32_t)K &&
-                          (tp.x != tp.y || ra < cb);
-                if (ok) {
-                    uint32_t s = 0;
-#pragma unroll
-                    for (int k = 0; k < kBins / 4; ++k) s = __vsadu4(pa[ra][k], pb[cb][k]) + s;
-                    ok = s <= thr;
-                }
+                const bool ok = (l1 != 0xffffffffu) && (l2 != 0xffffffffu) && dl <= (uint32_t)K &&
+                                (tp.x != tp.y || ra < cb) && l1s[r][c] <= thr;
                 mask |= (uint64_t)(ok ? 1u : 0u) << (r * 8 + c);
             }
         }

@@ -170,7 +170,7 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
                           &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
                           &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
-                          &c->items, &c->items_tmp, &c->sched_tmp};
+                          &c->items, &c->items_tmp, &c->sched_tmp, &c->sym};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

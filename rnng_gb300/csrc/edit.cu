@@ -301,6 +301,134 @@ __global__ void __launch_bounds__(256) k_edit_verify(const uint8_t* __restrict__
     }
 }
 
+// One 64-bit block of Myers' column step (G. Myers, J. ACM 46(3), 1999, block form):
+// vertical deltas (pv, mv) of 64 pattern rows against one text character with match
+// vector eq and horizontal delta hin entering at the block's top row; returns the
+// horizontal delta leaving the block at row bit `hb`.
+__device__ __forceinline__ int myers_block(unsigned long long eq, unsigned long long& pv, unsigned long long& mv,
+                                           int hin, unsigned long long hb)
+{
+    const unsigned long long neg = hin < 0 ? 1ull : 0ull, pos = hin > 0 ? 1ull : 0ull;
+    const unsigned long long xv = eq | mv;
+    eq |= neg;
+    const unsigned long long xh = (((eq & pv) + pv) ^ pv) | eq;
+    unsigned long long ph = mv | ~(xh | pv);
+    unsigned long long mh = pv & xh;
+    const int hout = (ph & hb) ? 1 : ((mh & hb) ? -1 : 0);
+    ph = (ph << 1) | pos;
+    mh = (mh << 1) | neg;
+    pv = mh | ~(xv | ph);
+    mv = ph & xv;
+    return hout;
+}
+
+constexpr int kBpMaxSym = 8;    // symbols of the compressed alphabet
+constexpr int kBpMaxLen = 128;  // pattern length (two 64-bit blocks)
+constexpr int kBpSlot = 2 * kBpMaxSym + 1;  // 64-bit words per thread slot (+1 against bank conflicts)
+
+// Verification by Myers' bit-vector algorithm: per candidate the shorter string is the
+// pattern (its match vectors per symbol of the dataset's alphabet, at most 8 symbols,
+// built in the thread's shared slot), the longer the text; the whole-string distance
+// is D[m][n] = m + the horizontal deltas leaving row m.  A column can lower the
+// distance by at most one, so the scan stops as soon as the distance cannot come back
+// to K.  Exact for every pair; used when the alphabet has at most 8 symbols and no
+// string is longer than 128 (otherwise k_edit_verify's banded DP runs).
+__global__ void __launch_bounds__(256) k_edit_verify_bp(const uint8_t* __restrict__ atoms,
+                                                        const int64_t* __restrict__ off,
+                                                        const int32_t* __restrict__ perm,
+                                                        const uint2* __restrict__ cand,
+                                                        const unsigned long long* __restrict__ ncand_ptr,
+                                                        unsigned long long ccap, int K,
+                                                        const uint8_t* __restrict__ symmap,
+                                                        uint32_t* __restrict__ eu, uint32_t* __restrict__ ev,
+                                                        float* __restrict__ ew, unsigned long long* __restrict__ ecount,
+                                                        unsigned long long cap)
+{
+    __shared__ unsigned long long peq_all[256 * kBpSlot];
+    __shared__ uint8_t smap[256];
+    __shared__ int s_warp[8];
+    __shared__ unsigned long long s_base;
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) smap[k] = symmap[k];
+    __syncthreads();
+    unsigned long long* peq = peq_all + threadIdx.x * kBpSlot;
+    const unsigned long long nc = min(*ncand_ptr, ccap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long round = (unsigned long long)blockIdx.x * blockDim.x; round < nc; round += stride) {
+        const unsigned long long e = round + threadIdx.x;
+        bool hit = false;
+        int dist = 0;
+        uint2 c = make_uint2(0, 0);
+        if (e < nc) {
+            c = cand[e];
+            const int64_t oa = off[perm[c.x]], ob = off[perm[c.y]];
+            const int ma = (int)(off[perm[c.x] + 1] - oa), mb = (int)(off[perm[c.y] + 1] - ob);
+            // the distance is symmetric: the shorter string is the pattern
+            const bool a_pat = ma <= mb;
+            const uint8_t* pat = atoms + (a_pat ? oa : ob);
+            const uint8_t* txt = atoms + (a_pat ? ob : oa);
+            const int m = a_pat ? ma : mb, n = a_pat ? mb : ma;
+            if (m == 0) {
+                dist = n;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 2 * kBpMaxSym; ++k) peq[k] = 0ull;
+                for (int i = 0; i < m; ++i) peq[2 * smap[pat[i]] + (i >> 6)] |= 1ull << (i & 63);
+                unsigned long long pv0 = ~0ull, mv0 = 0ull, pv1 = ~0ull, mv1 = 0ull;
+                const unsigned long long last = 1ull << ((m - 1) & 63);
+                int score = m;
+                if (m <= 64) {
+                    for (int j = 0; j < n; ++j) {
+                        const int sym = smap[txt[j]];
+                        score += myers_block(peq[2 * sym], pv0, mv0, 1, last);
+                        if (score > K + (n - 1 - j)) break;
+                    }
+                } else {
+                    for (int j = 0; j < n; ++j) {
+                        const int sym = smap[txt[j]];
+                        const int h0 = myers_block(peq[2 * sym], pv0, mv0, 1, 1ull << 63);
+                        score += myers_block(peq[2 * sym + 1], pv1, mv1, h0, last);
+                        if (score > K + (n - 1 - j)) break;
+                    }
+                }
+                dist = score;
+            }
+            hit = dist <= K;
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) s_warp[warp] = __popc(ball);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int a = 0;
+            for (int k = 0; k < 8; ++k) { const int t = s_warp[k]; s_warp[k] = a; a += t; }
+            s_base = a ? atomicAdd(ecount, (unsigned long long)a) : 0ull;
+        }
+        __syncthreads();
+        if (hit) {
+            const unsigned long long pos = s_base + s_warp[warp] + __popc(ball & ((1u << lane) - 1u));
+            if (pos < cap) {
+                eu[pos] = c.x;
+                ev[pos] = c.y;
+                ew[pos] = (float)dist;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Byte histogram of the strings (the alphabet of the bit-parallel verification).
+__global__ void k_byte_hist(const uint8_t* __restrict__ atoms, int64_t natoms, unsigned int* __restrict__ hist)
+{
+    __shared__ unsigned int h[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < natoms; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[atoms[i]], 1u);
+    __syncthreads();
+    for (int k = threadIdx.x; k < 256; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
 __global__ void k_edit_finalize(const uint32_t* __restrict__ si, const uint32_t* __restrict__ sj,
                                 const float* __restrict__ sw, int64_t m, const int32_t* __restrict__ perm,
                                 const int64_t* __restrict__ ids, int64_t* __restrict__ u, int64_t* __restrict__ v,
@@ -530,7 +658,39 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             }
             c->cand_cap_hint = std::max<unsigned long long>(c->cand_cap_hint, got + got / 8);
             c->stats.candidates = (int64_t)got;
-            // 4. exact banded verification
+            // 4. exact verification: Myers' bit-vector algorithm when the alphabet has at most
+            //    kBpMaxSym symbols and no string is longer than kBpMaxLen, else the banded DP
+            bool use_bp = false;
+            if (got > 0) {
+                uint32_t maxlen = 0;
+                int64_t total_atoms = 0;
+                RNNG_CUDA(cudaMemcpyAsync(&maxlen, slen + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaMemcpyAsync(&total_atoms, doff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                RNNG_CUDA(cudaStreamSynchronize(s));
+                if (maxlen <= (uint32_t)kBpMaxLen) {
+                    c->sym.reserve(256 * sizeof(unsigned int) + 256);
+                    unsigned int* hist = c->sym.as<unsigned int>();
+                    uint8_t* symmap = (uint8_t*)(hist + 256);
+                    RNNG_CUDA(cudaMemsetAsync(hist, 0, 256 * sizeof(unsigned int), s));
+                    const int64_t natoms_all = total_atoms;  // offsets start at 0 (RNNG's layout)
+                    if (natoms_all > 0) {
+                        k_byte_hist<<<(unsigned)std::min<int64_t>(ceil_div(natoms_all, 256), (int64_t)c->num_sms * 4),
+                                      256, 0, s>>>(datoms, natoms_all, hist);
+                        ++c->launches;
+                    }
+                    unsigned int h[256];
+                    RNNG_CUDA(cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, s));
+                    RNNG_CUDA(cudaStreamSynchronize(s));
+                    uint8_t map[256];
+                    int nsym = 0;
+                    for (int b = 0; b < 256; ++b) map[b] = h[b] ? (uint8_t)(nsym++) : (uint8_t)0;
+                    if (nsym <= kBpMaxSym) {
+                        RNNG_CUDA(cudaMemcpyAsync(symmap, map, 256, cudaMemcpyHostToDevice, s));
+                        RNNG_CUDA(cudaStreamSynchronize(s));  // map lifetime
+                        use_bp = true;
+                    }
+                }
+            }
             unsigned long long ecap = std::max<unsigned long long>(1u << 20, c->edge_cap_hint);
             unsigned long long egot = 0;
             const unsigned gv = (unsigned)std::max<unsigned long long>(
@@ -544,7 +704,11 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
                     auto* eu = c->edges_u.as<uint32_t>();
                     auto* ev = c->edges_v.as<uint32_t>();
                     auto* ew = c->edges_w.as<float>();
-                    if (K <= 4)
+                    if (use_bp)
+                        k_edit_verify_bp<<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap, K,
+                                                            (const uint8_t*)(c->sym.as<unsigned int>() + 256), eu, ev,
+                                                            ew, ecount, ecap);
+                    else if (K <= 4)
                         k_edit_verify<4><<<gv, 256, 0, s>>>(datoms, doff, perm, c->cand.as<uint2>(), ccount, ccap, K,
                                                             eu, ev, ew, ecount, ecap);
                     else if (K <= 8)

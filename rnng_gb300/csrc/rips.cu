@@ -21,6 +21,11 @@
 //      of its edges, which equals RNNG's recursive max over facets;
 //   7. all simplices sorted by (value, id).  Each simplex is built exactly once, so the
 //      merge's unique-by-id step (include/simplex.hpp:173-174) has nothing to remove.
+// Up to triangles over distinct ids small enough that RNNG's binomials are exact, the
+// ids are the combinatorial number system, so colex order of vertex tuples is id order:
+// edges are then keyed (larger, smaller), triangles found per edge (b, c) among the
+// lower neighbours of c below b and of b, in (c, b, a) order, and steps 2-3 emit every
+// simplex already in id order; step 7 is one stable 32-bit pass by value.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -136,9 +141,9 @@ __global__ void k_triangles(const uint64_t* __restrict__ key, const float* __res
 }
 
 __global__ void k_vertices_edges(const int64_t* __restrict__ id_of_rank, int64_t n, const uint64_t* __restrict__ key,
-                                 const float* __restrict__ w, int64_t m, bool with_edges, int64_t* __restrict__ out_id,
-                                 float* __restrict__ out_val, const uint8_t* __restrict__ fr,
-                                 uint8_t* __restrict__ out_flag)
+                                 const float* __restrict__ w, int64_t m, bool with_edges, bool colex,
+                                 int64_t* __restrict__ out_id, float* __restrict__ out_val,
+                                 const uint8_t* __restrict__ fr, uint8_t* __restrict__ out_flag)
 {
     const int64_t total = n + (with_edges ? m : 0);
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -148,11 +153,64 @@ __global__ void k_vertices_edges(const int64_t* __restrict__ id_of_rank, int64_t
             if (out_flag) out_flag[t] = fr[t];
         } else {
             const int64_t e = t - n;
-            const uint32_t a = (uint32_t)(key[e] >> 32), b = (uint32_t)(key[e] & 0xffffffffu);
+            const uint32_t hi = (uint32_t)(key[e] >> 32), lo = (uint32_t)(key[e] & 0xffffffffu);
+            const uint32_t a = colex ? lo : hi, b = colex ? hi : lo;  // a < b
             out_id[t] = simplex_id2(id_of_rank[a], id_of_rank[b]);
             out_val[t] = w[e];
             if (out_flag) out_flag[t] = fr[a] | fr[b];
         }
+    }
+}
+
+// (a << 32 | b) -> (b << 32 | a): edge keys by (larger rank, smaller rank).
+__global__ void k_swap_key_halves(uint64_t* __restrict__ key, int64_t m)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = key[e];
+        key[e] = (k << 32) | (k >> 32);
+    }
+}
+
+// Triangles in colex order (c, b, a), for keys sorted by (c, b) with c > b and a CSR of
+// lower neighbours: for edge e = (b < c) the lower neighbours of c before b (CSR
+// positions row[c] .. e - 1) intersected with the lower neighbours of b.  Edges in key
+// order and a ascending give the triangles sorted by their ids whenever RNNG's binomials
+// do not wrap.  Counts (emit == false) or writes ids, values (largest edge) and flags.
+template <bool emit>
+__global__ void k_triangles_colex(const uint64_t* __restrict__ key, const float* __restrict__ w,
+                                  const int32_t* __restrict__ row, int64_t m, const int64_t* __restrict__ id_of_rank,
+                                  int64_t* __restrict__ cnt, const int64_t* __restrict__ off,
+                                  int64_t* __restrict__ out_id, float* __restrict__ out_val,
+                                  const uint8_t* __restrict__ fr, uint8_t* __restrict__ out_flag)
+{
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(key[e] >> 32), b = (uint32_t)(key[e] & 0xffffffffu);
+        int64_t x = row[c];
+        const int64_t xe = e;
+        int64_t y = row[b];
+        const int64_t ye = row[b + 1];
+        const float wbc = w[e];
+        int64_t pos = emit ? off[e] : 0;
+        int64_t found = 0;
+        while (x < xe && y < ye) {
+            const uint32_t ax = (uint32_t)(key[x] & 0xffffffffu), ay = (uint32_t)(key[y] & 0xffffffffu);
+            if (ax < ay) {
+                ++x;
+            } else if (ax > ay) {
+                ++y;
+            } else {
+                if (emit) {
+                    out_id[pos] = simplex_id3(id_of_rank[ax], id_of_rank[b], id_of_rank[c]);
+                    out_val[pos] = fmaxf(fmaxf(wbc, w[x]), w[y]);
+                    if (out_flag) out_flag[pos] = fr[ax] | fr[b] | fr[c];
+                    ++pos;
+                }
+                ++found;
+                ++x;
+                ++y;
+            }
+        }
+        if (!emit) cnt[e] = found;
     }
 }
 
@@ -162,6 +220,16 @@ __global__ void k_flag_by_rank(const uint8_t* __restrict__ flag, const int32_t* 
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         fr[rank[i]] = flag[i] ? 1 : 0;
+}
+
+// Sets *bad unless the ranked ids are strictly increasing and within [0, max_id].
+__global__ void k_ids_colex(const int64_t* __restrict__ id_of_rank, int64_t n, int64_t max_id,
+                            unsigned int* __restrict__ bad)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t id = id_of_rank[r];
+        if (id < 0 || id > max_id || (r > 0 && id <= id_of_rank[r - 1])) atomicOr(bad, 1u);
+    }
 }
 
 __global__ void k_value_bits(const float* __restrict__ v, int64_t m, uint32_t* __restrict__ bits,
@@ -292,6 +360,7 @@ unsigned grid_for(rnng_ctx* c, int64_t work)
 struct Ranks {
     int64_t* id_of_rank;  // id of the vertex of rank r
     int32_t* rank;        // rank of row i
+    bool rows_are_ids;    // no ids given: the id of row i is i
 };
 
 // Vertices ranked by id (rows themselves without ids): rank order is id order, so
@@ -303,7 +372,7 @@ Ranks rank_vertices(rnng_ctx* c, const int64_t* dids, int64_t n)
     c->aux0.reserve(sizeof(int64_t) * 2 * (size_t)ng);
     c->aux1.reserve(sizeof(int32_t) * 3 * (size_t)ng + 16);
     int64_t* idk = c->aux0.as<int64_t>();
-    Ranks R{idk + ng, nullptr};
+    Ranks R{idk + ng, nullptr, dids == nullptr};
     int32_t* rows = c->aux1.as<int32_t>();
     int32_t* row_of_rank = rows + ng;
     R.rank = row_of_rank + ng;
@@ -369,6 +438,57 @@ int64_t scan_counts(rnng_ctx* c, int64_t* cnt, int64_t* off, int64_t count)
     return total;
 }
 
+// True when, for vertex ids in [0, max_id], RNNG's Binom (a 64-bit falling product,
+// include/utils.hpp:116-144) is exact for every binomial of a simplex id up to maxdim
+// (<= 2) and every id of dimension k stays below the dimension bits (below 2^60).  The
+// ids are then the combinatorial number system: colex order of vertex tuples is id
+// order within a dimension, and dimension k sorts before k + 1.
+bool colex_ids_exact(int64_t max_id, int maxdim)
+{
+    if (max_id < 0) return true;
+    if (max_id >= (int64_t(1) << 40)) return false;  // keeps the products below in 128 bits
+    using u128 = unsigned __int128;
+    const u128 M = (u128)max_id;
+    for (int k = 1; k <= maxdim + 1; ++k) {
+        u128 fall = 1, top = 1, fact = 1;  // M (M-1) ... (M-k+1); (M+1) M ... (M-k+2); k!
+        for (int i = 0; i < k; ++i) {
+            fall *= (M >= (u128)i) ? M - i : 0;
+            top *= M + 1 - i;
+            fact *= (u128)(i + 1);
+        }
+        if (fall >= ((u128)1 << 63)) return false;       // Binom's signed division stays exact
+        if (top / fact > ((u128)1 << 60)) return false;  // largest id of dimension k-1 is C(M+1, k) - 1
+    }
+    return true;
+}
+
+// Largest vertex id for which colex_ids_exact(., maxdim) holds.
+int64_t colex_max_id(int maxdim)
+{
+    int64_t lo = 0, hi = int64_t(1) << 40;
+    while (lo < hi) {
+        const int64_t mid = lo + (hi - lo + 1) / 2;
+        if (colex_ids_exact(mid, maxdim)) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Whether the simplices can be generated directly in id order (maxdim <= 2, distinct
+// ids within colex_max_id).  Without ids the rows 0..n-1 are the ids.
+bool colex_order(rnng_ctx* c, const Ranks& R, int64_t n, int maxdim)
+{
+    if (maxdim > 2) return false;
+    const int64_t bound = colex_max_id(maxdim);
+    if (n == 0) return true;
+    if (R.rows_are_ids) return n - 1 <= bound;
+    unsigned int* bad = (unsigned int*)(c->counters.as<unsigned long long>() + 11);
+    RNNG_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned int), c->stream));
+    k_ids_colex<<<grid_for(c, n), 256, 0, c->stream>>>(R.id_of_rank, n, bound, bad);
+    ++c->launches;
+    return read_flag(c, bad) == 0;
+}
+
 constexpr int64_t kMaxSimplices = (int64_t(1) << 31) - 1;
 
 // The filtration of the graph given by m unsorted rank-space keys (K.k0, K.w0) over n
@@ -391,7 +511,16 @@ void rips_from_keys(rnng_ctx* c, int64_t n, const Ranks& R, const Keys& K, int64
             ++c->launches;
         }
     }
-    // ---- sorted keys and the CSR of higher-ranked neighbours
+    // Up to triangles over small distinct ids, simplices are generated in id order:
+    // edges keyed (larger, smaller) and sorted, a CSR of lower neighbours, triangles per
+    // edge in colex order.  Otherwise (higher cliques, large or repeated ids) keys are
+    // (smaller, larger) with a CSR of higher neighbours, and the ids are sorted.
+    const bool colex = colex_order(c, R, n, maxdim);
+    if (colex && m > 0) {
+        k_swap_key_halves<<<grid_for(c, m), 256, 0, s>>>(K.k0, m);
+        ++c->launches;
+    }
+    // ---- sorted keys and the CSR of neighbours
     c->aux3.reserve(sizeof(int32_t) * 2 * ((size_t)ng + 1) + sizeof(int64_t) * 2 * ((size_t)mg + 1) + 64);
     int32_t* deg = c->aux3.as<int32_t>();
     int32_t* rowp = deg + ng + 1;
@@ -416,8 +545,12 @@ void rips_from_keys(rnng_ctx* c, int64_t n, const Ranks& R, const Keys& K, int64
         ++c->launches;
         exclusive_scan_i32(c, deg, rowp, n + 1);
         if (maxdim >= 2) {
-            k_triangles<false><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, tcnt, nullptr, nullptr,
-                                                             nullptr, nullptr, nullptr, nullptr);
+            if (colex)
+                k_triangles_colex<false><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, tcnt,
+                                                                       nullptr, nullptr, nullptr, nullptr, nullptr);
+            else
+                k_triangles<false><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, tcnt, nullptr,
+                                                                 nullptr, nullptr, nullptr, nullptr, nullptr);
             ++c->launches;
             ntri = scan_counts(c, tcnt, toff, m);
         }
@@ -435,9 +568,14 @@ void rips_from_keys(rnng_ctx* c, int64_t n, const Ranks& R, const Keys& K, int64
             c->clq0.reserve(sizeof(int32_t) * 3 * (size_t)ntri);
             clq = c->clq0.as<int32_t>();
         }
-        k_triangles<true><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, nullptr, toff,
-                                                        c->hi_id.as<int64_t>(), c->hi_val.as<float>(), clq, fr,
-                                                        with_flags ? c->hi_flag.as<uint8_t>() : nullptr);
+        if (colex)
+            k_triangles_colex<true><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, nullptr, toff,
+                                                                  c->hi_id.as<int64_t>(), c->hi_val.as<float>(), fr,
+                                                                  with_flags ? c->hi_flag.as<uint8_t>() : nullptr);
+        else
+            k_triangles<true><<<grid_for(c, m), 256, 0, s>>>(K.k1, K.w1, rowp, m, R.id_of_rank, nullptr, toff,
+                                                            c->hi_id.as<int64_t>(), c->hi_val.as<float>(), clq, fr,
+                                                            with_flags ? c->hi_flag.as<uint8_t>() : nullptr);
         ++c->launches;
         nhi = ntri;
         int64_t nc = ntri;   // cliques of the last level: k ranks each in *cur
@@ -496,8 +634,8 @@ void rips_from_keys(rnng_ctx* c, int64_t n, const Ranks& R, const Keys& K, int64
         f1 = f0 + tg;
     }
     if (n + nedge > 0) {
-        k_vertices_edges<<<grid_for(c, n + nedge), 256, 0, s>>>(R.id_of_rank, n, K.k1, K.w1, m, maxdim >= 1, id0, v0,
-                                                                fr, f0);
+        k_vertices_edges<<<grid_for(c, n + nedge), 256, 0, s>>>(R.id_of_rank, n, K.k1, K.w1, m, maxdim >= 1, colex,
+                                                                id0, v0, fr, f0);
         ++c->launches;
     }
     if (nhi > 0) {
@@ -509,8 +647,50 @@ void rips_from_keys(rnng_ctx* c, int64_t n, const Ranks& R, const Keys& K, int64
     int64_t* ids_out = id0;
     float* vals_out = v0;
     uint8_t* flags_out = f0;
-    if (total > 1) {
-        // stable passes: by id, then by value bits
+    // Values are >= +0, so their bits sort in numeric order; every radix pass is stable.
+    if (total > 1 && colex) {
+        // already in id order: one pass by value
+        const unsigned gt = grid_for(c, total);
+        size_t tmp = 0;
+        if (!with_flags) {
+            const uint32_t* kin = (const uint32_t*)v0;
+            uint32_t* kout = (uint32_t*)v1;
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kin, kout, id0, id1, (int)total, 0, 32, s));
+            c->cub_tmp.reserve(tmp);
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, kin, kout, id0, id1, (int)total, 0, 32, s));
+            c->launches += cub_sort_kernels(total, 32);
+        } else {
+            k_value_bits<<<gt, 256, 0, s>>>(v0, total, b0, p0);
+            ++c->launches;
+            uint32_t* kout = (uint32_t*)v1;
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, b0, kout, p0, p1, (int)total, 0, 32, s));
+            c->cub_tmp.reserve(tmp);
+            RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, b0, kout, p0, p1, (int)total, 0, 32, s));
+            c->launches += cub_sort_kernels(total, 32);
+            k_permute<int64_t><<<gt, 256, 0, s>>>(id0, p1, total, id1);
+            k_permute<uint8_t><<<gt, 256, 0, s>>>(f0, p1, total, f1);
+            c->launches += 2;
+            flags_out = f1;
+        }
+        ids_out = id1;
+        vals_out = v1;
+    } else if (total > 1 && !with_flags) {
+        // by id carrying the value bits, then by value bits carrying the ids
+        size_t tmp = 0;
+        const uint32_t* bin = (const uint32_t*)v0;
+        uint32_t* vout = (uint32_t*)v1;
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, id0, id1, bin, b1, (int)total, 0, 64, s));
+        c->cub_tmp.reserve(tmp);
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, id0, id1, bin, b1, (int)total, 0, 64, s));
+        c->launches += cub_sort_kernels(total, 64);
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, b1, vout, id1, id0, (int)total, 0, 32, s));
+        c->cub_tmp.reserve(tmp);
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, b1, vout, id1, id0, (int)total, 0, 32, s));
+        c->launches += cub_sort_kernels(total, 32);
+        ids_out = id0;
+        vals_out = v1;
+    } else if (total > 1) {
+        // stable passes: by id, then by value bits, carrying positions for the flags
         const unsigned gt = grid_for(c, total);
         size_t tmp = 0;
         k_value_bits<<<gt, 256, 0, s>>>(v0, total, b0, p0);

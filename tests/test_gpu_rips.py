@@ -37,7 +37,7 @@ def test_golden_edit_rips_through_edges(ctx):
     assert same(got, (g["ids"], g["values"]))
 
 
-@pytest.mark.parametrize("maxdim", [3, 4, 6])
+@pytest.mark.parametrize("maxdim", [2, 3, 4, 6])
 def test_higher_dimensions_against_oracle(ctx, orc, maxdim):
     rng = np.random.default_rng(maxdim + 70)
     x = rng.normal(size=(700, 3)).astype(np.float32)
@@ -118,29 +118,65 @@ def test_random_against_oracle(ctx, orc, maxdim):
     assert same(ctx.rips_l2(x, r, maxdim=maxdim), want)
 
 
-def test_ids_and_edge_cases(ctx, orc):
-    rng = np.random.default_rng(60)
-    x = rng.normal(size=(400, 3)).astype(np.float32)
-    r = np.float32(0.9)
-    ids = rng.permutation(400).astype(np.int64) * 11 + 5
-    gi, gv = ctx.rips_l2(x, r, maxdim=2, ids=ids)
-    # expected filtration over the labels: vertices, edges and triangles by brute force
+def colex_max_id(maxdim: int = 2) -> int:
+    """Largest vertex id for which every simplex id up to maxdim is an exact binomial sum
+    below the dimension bits (the library then builds simplices in id order)."""
+    from math import comb, perm
+
+    def exact(m):
+        return all(perm(m, k) < 2 ** 63 and comb(m + 1, k) <= 2 ** 60 for k in range(1, maxdim + 2))
+    lo, hi = 0, 1 << 40
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        lo, hi = (mid, hi) if exact(mid) else (lo, mid - 1)
+    return lo
+
+
+def brute_filtration(orc, x, r, labels):
+    """Vertices, edges and triangles over rows, ids from the rows' labels, sorted by
+    (value, id); equal (value, id) records are identical, so the sequence is unique."""
     u, v, w = orc.eps_graph_l2(x, r)
-    wmap = {}
-    for a, b, c in zip(ids[u].tolist(), ids[v].tolist(), w.tolist()):
-        wmap[(min(a, b), max(a, b))] = c
+    wmap = {(a, b): c for a, b, c in zip(u.tolist(), v.tolist(), w.tolist())}
     adj = {}
     for (a, b) in wmap:
         adj.setdefault(a, set()).add(b)
-    want = [(0.0, orc.simplex_id([i])) for i in ids.tolist()]
-    want += [(c, orc.simplex_id([a, b])) for (a, b), c in wmap.items()]
+    lab = labels.tolist()
+    want = [(0.0, orc.simplex_id([i])) for i in lab]
+    want += [(c, orc.simplex_id([lab[a], lab[b]])) for (a, b), c in wmap.items()]
     for a in adj:
         for b in adj[a]:
             for c in adj[a] & adj.get(b, set()):
-                want.append((max(wmap[(a, b)], wmap[(a, c)], wmap[(b, c)]), orc.simplex_id([a, b, c])))
+                want.append((max(wmap[(a, b)], wmap[(a, c)], wmap[(b, c)]), orc.simplex_id([lab[a], lab[b], lab[c]])))
     want.sort()
-    assert gi.tolist() == [t for _, t in want]
-    assert np.array_equal(gv, np.array([val for val, _ in want], np.float32))
+    return [t for _, t in want], np.array([val for val, _ in want], np.float32)
+
+
+@pytest.mark.parametrize("labels", ["spread", "at_bound", "above_bound", "beyond_wrap", "negative", "repeated"])
+def test_ids_against_brute_force(ctx, orc, labels):
+    """Ids that allow generation in id order (spread, at_bound) and ids that need the
+    general sort (above the exact-binomial bound, wrapping binomials, negative or
+    repeated ids) give the same filtration as a brute-force enumeration."""
+    rng = np.random.default_rng(60)
+    x = rng.normal(size=(400, 3)).astype(np.float32)
+    r = np.float32(0.9)
+    p = rng.permutation(400).astype(np.int64)
+    bound = colex_max_id(2)
+    ids = {"spread": p * 11 + 5, "at_bound": p + (bound - 399), "above_bound": p + (bound - 398),
+           "beyond_wrap": p + 3_000_000, "negative": p - 200,
+           "repeated": rng.integers(0, 150, size=400).astype(np.int64)}[labels]
+    gi, gv = ctx.rips_l2(x, r, maxdim=2, ids=ids)
+    wi, wv = brute_filtration(orc, x, r, ids)
+    assert gi.tolist() == wi
+    assert np.array_equal(gv.view(np.uint32), wv.view(np.uint32))
+    # the same through the edge-list entry point, with flags
+    u, v, w = orc.eps_graph_l2(x, r)
+    fi, fv, ff = ctx.rips_edges(400, u, v, w, maxdim=2, ids=ids, vertex_flags=np.ones(400, np.uint8))
+    assert fi.tolist() == wi and np.array_equal(fv.view(np.uint32), wv.view(np.uint32)) and np.all(ff == 1)
+
+
+def test_edge_cases(ctx):
+    rng = np.random.default_rng(61)
+    x = rng.normal(size=(400, 3)).astype(np.float32)
     # duplicates collapse to zero-length edges and triangles at value 0
     y = np.ones((10, 4), np.float32)
     yi, yv = ctx.rips_l2(y, 0.0, maxdim=2)

@@ -50,6 +50,9 @@ constexpr int kEpiGroups = 2;                       // epilogue groups, taking a
 constexpr int kGroupWarps = 8;                      // per group: 2 per TMEM sub-partition
 constexpr int kEpiWarps = kEpiGroups * kGroupWarps;
 constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 576
+// 18 warps put five on two SM sub-partitions (16K registers each): at most 96 per thread.
+// __maxnreg__ rather than __launch_bounds__: at the same 96 the latter's allocation spills.
+constexpr int kGramMaxRegs = 96;
 constexpr int kEpiCols = kAccCols / (kGroupWarps / 4);  // accumulator columns per epilogue warp (64)
 constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
 constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared memory per block (227 KB)
@@ -212,6 +215,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
     for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// Three-input minimum (exact, like fminf(fminf(a, b), c)).
+__device__ __forceinline__ float min3f(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row core
 // groups 1024 bytes apart (SBO), descriptor version 1 (sm_100 family).
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
@@ -278,7 +289,7 @@ struct ItemPrefetch {
 // same time (B tiles are shared through L2).
 
 template <int KCH, int NT>  // KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item
-__global__ void __launch_bounds__(kGramThreads, 1)
+__global__ void __maxnreg__(kGramMaxRegs)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int4* __restrict__ items, unsigned long long nitems,
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
@@ -339,9 +350,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
             uint32_t aloads = 0;
             int cur_i = -1;
-            uint32_t last_phase[kMaxSlots];
-            bool issued[kMaxSlots];
-            for (int q = 0; q < kMaxSlots; ++q) { issued[q] = false; last_phase[q] = 0; }
+            uint32_t issued = 0, last_phase = 0;  // per ring slot: loads issued, phase of the last
             bool ok = true;
             ItemPrefetch pf;
             pf.init(items, wbeg, wend);
@@ -370,8 +379,8 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                     if (second)
                         tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, it.z * kTile);
                 }
-                issued[q] = true;
-                last_phase[q] = ph;
+                issued |= 1u << q;
+                last_phase = (last_phase & ~(1u << q)) | (ph << q);
                 if (++q == nslots) {
                     q = 0;
                     ph ^= 1u;
@@ -384,9 +393,9 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                     while (!mbar_try_wait(a_full, (aloads - 1) & 1u) && globaltimer() - t0 < kWaitNs) {
                     }
                 for (int qq = 0; qq < kMaxSlots; ++qq) {
-                    if (!issued[qq]) continue;
+                    if (!((issued >> qq) & 1u)) continue;
                     t0 = globaltimer();
-                    while (!mbar_try_wait(&b_full[qq], last_phase[qq]) && globaltimer() - t0 < kWaitNs) {
+                    while (!mbar_try_wait(&b_full[qq], (last_phase >> qq) & 1u) && globaltimer() - t0 < kWaitNs) {
                     }
                 }
             }
@@ -471,42 +480,45 @@ __global__ void __launch_bounds__(kGramThreads, 1)
         const int r = sub * 32 + lane;
         ItemPrefetch pf;
         pf.init(items, ubeg, wend, ustride);
-        // row / column data of the current unit, loaded one unit ahead
-        int4 it = pf.next(ubeg);
+        // row / column data of the current unit, loaded one unit ahead; of an item only its
+        // row tile and this group's column tile are kept (it_i, it_j)
+        int it_i, it_j;
+        {
+            const int4 it = pf.next(ubeg);
+            it_i = it.x;
+            it_j = half ? it.z : it.y;
+        }
         float2 uc = make_float2(0.f, 0.f);
         float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
         float2 tj = make_float2(0.f, 0.f);
-        {
-            const int jt = half ? it.z : it.y;
-            if (ubeg < wend && jt >= 0) {
-                uc = reinterpret_cast<const float2*>(ucol)[((int64_t)jt * kTile + cg * kEpiCols) / 2 + lane];
-                ri = rowinfo[(int64_t)it.x * kTile + r];
-                tj = tileinfo[jt];
-            }
+        if (ubeg < wend && it_j >= 0) {
+            uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
+            ri = rowinfo[(int64_t)it_i * kTile + r];
+            tj = tileinfo[it_j];
         }
         uint32_t local = (uint32_t)(ubeg - wbeg);  // item index within the CTA's range
         for (unsigned long long w = ubeg; w < wend; w += ustride, local += ustride) {
             const int b = (int)(local % (uint32_t)kAcc);
             const uint32_t tph = (local / (uint32_t)kAcc) & 1u;
-            const int jt = half ? it.z : it.y;  // this unit's column tile (-1: none)
+            const int jt = it_j;  // this unit's column tile (-1: none)
             const int64_t j0 = (int64_t)jt * kTile + cg * kEpiCols;
-            const int64_t gi = (int64_t)it.x * kTile + r;
-            const bool diag = it.x == jt;
+            const int64_t gi = (int64_t)it_i * kTile + r;
+            const bool diag = it_i == jt;
             reinterpret_cast<float2*>(colu)[lane] = uc;
             const float A = eps_p + ri.y;
             const float AA = A * A, cross = 2.f * A * tj.x;
             const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
             // issue the next unit's loads now; they complete while this one is tested
-            const int4 itn = pf.next(w + ustride);
             {
-                const int jn = half ? itn.z : itn.y;
-                if (w + ustride < wend && jn >= 0) {
-                    uc = reinterpret_cast<const float2*>(ucol)[((int64_t)jn * kTile + cg * kEpiCols) / 2 + lane];
-                    ri = rowinfo[(int64_t)itn.x * kTile + r];
-                    tj = tileinfo[jn];
+                const int4 itn = pf.next(w + ustride);
+                it_i = itn.x;
+                it_j = half ? itn.z : itn.y;
+                if (w + ustride < wend && it_j >= 0) {
+                    uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
+                    ri = rowinfo[(int64_t)it_i * kTile + r];
+                    tj = tileinfo[it_j];
                 }
             }
-            it = itn;
             __syncwarp();
             // fast path: the accumulator is usually ready; otherwise lane 0 waits (bounded)
             if (!__all_sync(0xffffffffu, mbar_try_wait(&tfull[b], tph))) {
@@ -537,14 +549,26 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                 }
                 // most rows have no candidate: test the minimum first
                 // four independent running minima keep the dependent chain short
+                // (packed pairs: __ffma2_rn forms two terms, each rounded once as fmaf; a three-input
+                // minimum takes two of them)
                 float m0 = INFINITY, m1 = INFINITY, m2 = INFINITY, m3 = INFINITY;
+                const float2 k2 = make_float2(-2.f, -2.f);
 #pragma unroll
                 for (int t4 = 0; t4 < 8; ++t4) {
                     const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
-                    m0 = fminf(m0, fmaf(-2.f, g[4 * t4 + 0], u4.x));
-                    m1 = fminf(m1, fmaf(-2.f, g[4 * t4 + 1], u4.y));
-                    m2 = fminf(m2, fmaf(-2.f, g[4 * t4 + 2], u4.z));
-                    m3 = fminf(m3, fmaf(-2.f, g[4 * t4 + 3], u4.w));
+                    const float2 p = __ffma2_rn(make_float2(g[4 * t4 + 0], g[4 * t4 + 1]), k2, make_float2(u4.x, u4.y));
+                    const float2 q = __ffma2_rn(make_float2(g[4 * t4 + 2], g[4 * t4 + 3]), k2, make_float2(u4.z, u4.w));
+                    g[4 * t4 + 0] = p.x;  // g now holds the terms -2 g + u_j
+                    g[4 * t4 + 1] = p.y;
+                    g[4 * t4 + 2] = q.x;
+                    g[4 * t4 + 3] = q.y;
+                    if (t4 & 1) {
+                        m0 = min3f(m0, p.x, p.y);
+                        m1 = min3f(m1, q.x, q.y);
+                    } else {
+                        m2 = min3f(m2, p.x, p.y);
+                        m3 = min3f(m3, q.x, q.y);
+                    }
                 }
                 const float mn = fminf(fminf(m0, m1), fminf(m2, m3));
                 const bool mine = mn <= Wi;
@@ -552,13 +576,7 @@ __global__ void __launch_bounds__(kGramThreads, 1)
                 uint32_t m = 0;
                 if (mine) {
 #pragma unroll
-                    for (int t4 = 0; t4 < 8; ++t4) {
-                        const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
-                        m |= (fmaf(-2.f, g[4 * t4 + 0], u4.x) <= Wi ? 1u : 0u) << (4 * t4 + 0);
-                        m |= (fmaf(-2.f, g[4 * t4 + 1], u4.y) <= Wi ? 1u : 0u) << (4 * t4 + 1);
-                        m |= (fmaf(-2.f, g[4 * t4 + 2], u4.z) <= Wi ? 1u : 0u) << (4 * t4 + 2);
-                        m |= (fmaf(-2.f, g[4 * t4 + 3], u4.w) <= Wi ? 1u : 0u) << (4 * t4 + 3);
-                    }
+                    for (int k = 0; k < 32; ++k) m |= (g[k] <= Wi ? 1u : 0u) << k;
                 }
                 const int64_t jc = j0 + ch * 32;
                 // padding rows / columns and, inside a diagonal tile, j <= i excluded

@@ -16,14 +16,16 @@
 // each candidate is then re-evaluated with the reference's sequential FP32 L2 in a
 // separate kernel: the edge set and every weight are exactly the reference's.
 //
-// Kernel roles (one CTA per SM, persistent over the tile-pair list):
+// Kernel roles (one CTA per SM, persistent over the scheduled items; an item is a row
+// tile with up to two column tiles):
 //   warp 0      TMA producer: the A tile (rows of I, all K-chunks of 64 BF16 = one
 //               128 B swizzle span each) into a resident buffer when I changes, and
-//               the B tile (rows of J, all K-chunks) into a ring of item slots
-//   warp 1      MMA issuer: 4 x (M=128, N=128, K=16) per chunk into one of four
-//               TMEM accumulators (4 x 128 columns), one commit per item
-//   warps 2-9   epilogue: 2 warps per TMEM sub-partition, each reads a 32 x 64
-//               slice of the accumulator (one lane per point of I), tests it and
+//               the B tiles (rows of J, all K-chunks) into a ring of item slots
+//   warp 1      MMA issuer: (M=128, N=128 per column tile, K=16) MMAs into one of the
+//               accumulators of 512 TMEM columns, one commit per item
+//   warps 2-17  epilogue, two groups of 8 (one column tile each): 2 warps per TMEM
+//               sub-partition, each reads its 32 x 64 slice of the accumulator in the
+//               16x256b fragment layout (4 rows x 16 columns per thread), tests it and
 //               appends candidates with one atomic per warp
 // Every mbarrier wait is bounded (about one second of wall time); on timeout the
 // CTA records a fault code in the context's fault word, stops issuing work, waits
@@ -198,22 +200,25 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar)
                  : "memory");
 }
 
-// 32 lanes x 32 consecutive fp32 columns: thread t receives row (lane base + t).
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+// tcgen05.ld.16x256b.x8 without the wait: 16 TMEM lanes x 64 columns.  Thread t gets,
+// for each 8-column block m (0..7), v[4m + 0, 1] = (lane t/4, columns 8m + 2(t%4) + 0, 1)
+// and v[4m + 2, 3] = (lane t/4 + 8, the same columns): the m16n8 accumulator fragment.
+__device__ __forceinline__ void tmem_ld16x256b_x8(uint32_t taddr, float* v)
 {
     uint32_t r[32];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%"
+        "tcgen05.ld.sync.aligned.16x256b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%"
         "19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
           "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Three-input minimum (exact, like fminf(fminf(a, b), c)).
 __device__ __forceinline__ float min3f(float a, float b, float c)
@@ -496,18 +501,31 @@ __global__ void __maxnreg__(kGramMaxRegs)
             ri = rowinfo[(int64_t)it_i * kTile + r];
             tj = tileinfo[it_j];
         }
+        // Fragment layout (tcgen05.ld.16x256b): thread (rq, q4) = (lane / 4, lane % 4) holds
+        // rows rq + 8 k (k = 0..3) of this sub-partition and columns 8 m + 2 q4 + e
+        // (m = 0..7, e = 0..1) of the warp's 64: 16 column terms u_j per thread and item
+        // (with a 32x32b load every thread would need all 64).
+        const int rq = lane >> 2, q4 = lane & 3;
+        const int n32 = (int)n;
+        const float2* colu2 = reinterpret_cast<const float2*>(colu);
         uint32_t local = (uint32_t)(ubeg - wbeg);  // item index within the CTA's range
         for (unsigned long long w = ubeg; w < wend; w += ustride, local += ustride) {
             const int b = (int)(local % (uint32_t)kAcc);
             const uint32_t tph = (local / (uint32_t)kAcc) & 1u;
             const int jt = it_j;  // this unit's column tile (-1: none)
-            const int64_t j0 = (int64_t)jt * kTile + cg * kEpiCols;
-            const int64_t gi = (int64_t)it_i * kTile + r;
+            // (indices fit int: n < 2^31 - 128 is checked at the boundary)
+            const int rb = it_i * kTile + sub * 32 + rq;          // row of k = 0
+            const int cb = jt * kTile + cg * kEpiCols + 2 * q4;   // column of m = e = 0, chunk 0
             const bool diag = it_i == jt;
             reinterpret_cast<float2*>(colu)[lane] = uc;
-            const float A = eps_p + ri.y;
-            const float AA = A * A, cross = 2.f * A * tj.x;
-            const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
+            float Wk[4];
+            {
+                const float A = eps_p + ri.y;
+                const float AA = A * A, cross = 2.f * A * tj.x;
+                const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) Wk[k] = __shfl_sync(0xffffffffu, Wi, rq + 8 * k);
+            }
             // issue the next unit's loads now; they complete while this one is tested
             {
                 const int4 itn = pf.next(w + ustride);
@@ -538,58 +556,53 @@ __global__ void __maxnreg__(kGramMaxRegs)
             }
             const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) +
                                    (uint32_t)(b * kAccCols * NT + half * kAccCols + cg * kEpiCols);
-            for (int ch = 0; ch < kEpiCols / 32; ++ch) {
+            // this thread's column terms: u2[m] = u_j of columns 8 m + 2 q4 + {0, 1}
+            float2 u2[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) u2[m] = colu2[4 * m + q4];
+            for (int hh = 0; hh < 2; ++hh) {
+                // lanes 16 hh .. 16 hh + 15 of the sub-partition, all 64 columns:
+                // g[4 m + 2 hi + e] = row rq + 8 hi + 16 hh, column 8 m + 2 q4 + e
                 float g[32];
-                tmem_ld32(taddr + ch * 32, g);
-                if (ch == kEpiCols / 32 - 1) {
+                tmem_ld16x256b_x8(taddr + ((uint32_t)(16 * hh) << 16), g);
+                tmem_ld_wait();
+                if (hh == 1) {
                     // accumulator slice read: hand it back to the MMA warp
                     tc_fence_before();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[b]);
                 }
-                // most rows have no candidate: test the minimum first
-                // four independent running minima keep the dependent chain short
-                // (packed pairs: __ffma2_rn forms two terms, each rounded once as fmaf; a three-input
-                // minimum takes two of them)
-                float m0 = INFINITY, m1 = INFINITY, m2 = INFINITY, m3 = INFINITY;
+                // most rows have no candidate: test each row's minimum first.  Packed pairs:
+                // __ffma2_rn forms two terms -2 g + u_j, each rounded once as fmaf; a
+                // three-input minimum takes both into one of the row's two running minima.
+                float mk[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
                 const float2 k2 = make_float2(-2.f, -2.f);
 #pragma unroll
-                for (int t4 = 0; t4 < 8; ++t4) {
-                    const float4 u4 = reinterpret_cast<const float4*>(colu)[ch * 8 + t4];
-                    const float2 p = __ffma2_rn(make_float2(g[4 * t4 + 0], g[4 * t4 + 1]), k2, make_float2(u4.x, u4.y));
-                    const float2 q = __ffma2_rn(make_float2(g[4 * t4 + 2], g[4 * t4 + 3]), k2, make_float2(u4.z, u4.w));
-                    g[4 * t4 + 0] = p.x;  // g now holds the terms -2 g + u_j
-                    g[4 * t4 + 1] = p.y;
-                    g[4 * t4 + 2] = q.x;
-                    g[4 * t4 + 3] = q.y;
-                    if (t4 & 1) {
-                        m0 = min3f(m0, p.x, p.y);
-                        m1 = min3f(m1, q.x, q.y);
-                    } else {
-                        m2 = min3f(m2, p.x, p.y);
-                        m3 = min3f(m3, q.x, q.y);
+                for (int m = 0; m < 8; ++m)
+#pragma unroll
+                    for (int hi = 0; hi < 2; ++hi) {
+                        const int x = 4 * m + 2 * hi;
+                        const float2 p = __ffma2_rn(make_float2(g[x], g[x + 1]), k2, u2[m]);
+                        g[x] = p.x;  // g now holds the terms
+                        g[x + 1] = p.y;
+                        mk[2 * hi + (m & 1)] = min3f(mk[2 * hi + (m & 1)], p.x, p.y);
                     }
-                }
-                const float mn = fminf(fminf(m0, m1), fminf(m2, m3));
-                const bool mine = mn <= Wi;
+                const float W0 = Wk[2 * hh], W1 = Wk[2 * hh + 1];
+                const bool mine = fminf(mk[0], mk[1]) <= W0 || fminf(mk[2], mk[3]) <= W1;
                 if (!__any_sync(0xffffffffu, mine)) continue;
-                uint32_t m = 0;
+                const int r0 = rb + 16 * hh;
+                uint32_t msk = 0;
                 if (mine) {
 #pragma unroll
-                    for (int k = 0; k < 32; ++k) m |= (g[k] <= Wi ? 1u : 0u) << k;
+                    for (int x = 0; x < 32; ++x) {
+                        const int gi = r0 + 8 * ((x >> 1) & 1);
+                        const int gj = cb + 8 * (x >> 2) + (x & 1);
+                        // padding rows / columns and, inside a diagonal tile, j <= i excluded
+                        const bool ok = g[x] <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
+                        msk |= (ok ? 1u : 0u) << x;
+                    }
                 }
-                const int64_t jc = j0 + ch * 32;
-                // padding rows / columns and, inside a diagonal tile, j <= i excluded
-                if (gi >= n) m = 0;
-                if (jc + 32 > n) {
-                    const int64_t lim = n - jc;
-                    m &= lim <= 0 ? 0u : (lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u));
-                }
-                if (diag) {
-                    const int64_t first = gi - jc + 1;
-                    m &= first <= 0 ? 0xffffffffu : (first >= 32 ? 0u : ~((1u << first) - 1u));
-                }
-                const int cnt = __popc(m);
+                const int cnt = __popc(msk);
                 int incl = cnt;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -602,10 +615,11 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     if (lane == 31) base = atomicAdd(cand_count, (unsigned long long)total);
                     base = __shfl_sync(0xffffffffu, base, 31);
                     unsigned long long pos = base + (unsigned long long)(incl - cnt);
-                    while (m) {
-                        const int t = __ffs(m) - 1;
-                        m &= m - 1;
-                        if (pos < cand_cap) cand[pos] = make_uint2((uint32_t)gi, (uint32_t)(jc + t));
+                    while (msk) {
+                        const int x = __ffs(msk) - 1;
+                        msk &= msk - 1;
+                        if (pos < cand_cap)
+                            cand[pos] = make_uint2((uint32_t)(r0 + 8 * ((x >> 1) & 1)), (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
                         ++pos;
                     }
                 }

@@ -56,6 +56,7 @@ constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 576
 // __maxnreg__ rather than __launch_bounds__: at the same 96 the latter's allocation spills.
 constexpr int kGramMaxRegs = 96;
 constexpr int kEpiCols = kAccCols / (kGroupWarps / 4);  // accumulator columns per epilogue warp (64)
+constexpr int kColuFloats = 80;                     // per epilogue warp: its 64 u_j in 4 padded rows of 20
 constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
 constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared memory per block (227 KB)
 
@@ -70,8 +71,8 @@ struct GramSmem {
     __host__ __device__ static GramSmem make(int kch, int nt)
     {
         GramSmem g;
-        g.colinfo = 0;                                     // kEpiWarps x kEpiCols floats (u_j)
-        g.bars = g.colinfo + kEpiWarps * kEpiCols * 4;     // mbarriers
+        g.colinfo = 0;                                     // kEpiWarps x kColuFloats floats (u_j)
+        g.bars = g.colinfo + kEpiWarps * kColuFloats * 4;  // mbarriers
         g.misc = g.bars + nbars * 8;                       // tmem slot, abort flag
         g.a_tile = (g.misc + 16 + 1023) & ~1023u;
         g.slot_bytes = (uint32_t)(kch * nt) * kChunkBytes;
@@ -481,7 +482,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
         const int half = NT == 2 ? grp : 0;
         const unsigned ustride = NT == 2 ? 1u : (unsigned)kEpiGroups;
         const unsigned long long ubeg = wbeg + (NT == 2 ? 0 : grp);
-        float* colu = (float*)(sm + SL.colinfo) + ew * kEpiCols;
+        float* colu = (float*)(sm + SL.colinfo) + ew * kColuFloats;
         const int r = sub * 32 + lane;
         ItemPrefetch pf;
         pf.init(items, ubeg, wend, ustride);
@@ -507,7 +508,6 @@ __global__ void __maxnreg__(kGramMaxRegs)
         // (with a 32x32b load every thread would need all 64).
         const int rq = lane >> 2, q4 = lane & 3;
         const int n32 = (int)n;
-        const float2* colu2 = reinterpret_cast<const float2*>(colu);
         uint32_t local = (uint32_t)(ubeg - wbeg);  // item index within the CTA's range
         for (unsigned long long w = ubeg; w < wend; w += ustride, local += ustride) {
             const int b = (int)(local % (uint32_t)kAcc);
@@ -517,7 +517,9 @@ __global__ void __maxnreg__(kGramMaxRegs)
             const int rb = it_i * kTile + sub * 32 + rq;          // row of k = 0
             const int cb = jt * kTile + cg * kEpiCols + 2 * q4;   // column of m = e = 0, chunk 0
             const bool diag = it_i == jt;
-            reinterpret_cast<float2*>(colu)[lane] = uc;
+            // staged for the fragment threads: column 8 m + 2 q + e at float 20 q + 2 m + e, so that
+            // thread (., q) reads its 16 terms as four 16-byte loads, the four q rows in distinct banks
+            reinterpret_cast<float2*>(colu)[(lane & 3) * 10 + (lane >> 2)] = uc;
             float Wk[4];
             {
                 const float A = eps_p + ri.y;
@@ -559,7 +561,11 @@ __global__ void __maxnreg__(kGramMaxRegs)
             // this thread's column terms: u2[m] = u_j of columns 8 m + 2 q4 + {0, 1}
             float2 u2[8];
 #pragma unroll
-            for (int m = 0; m < 8; ++m) u2[m] = colu2[4 * m + q4];
+            for (int t = 0; t < 4; ++t) {
+                const float4 v = reinterpret_cast<const float4*>(colu + 20 * q4)[t];
+                u2[2 * t] = make_float2(v.x, v.y);
+                u2[2 * t + 1] = make_float2(v.z, v.w);
+            }
             for (int hh = 0; hh < 2; ++hh) {
                 // lanes 16 hh .. 16 hh + 15 of the sub-partition, all 64 columns:
                 // g[4 m + 2 hi + e] = row rq + 8 hi + 16 hh, column 8 m + 2 q4 + e

@@ -298,6 +298,8 @@ def main():
                                   "edges": int(edges), "tile_pairs": int(last["tile_pairs"]),
                                   "tile_pairs_all": int(last["tile_pairs_all"]),
                                   "candidates": int(last["candidates"]),
+                                  "prune": {"tensor_cores": bool(last["prune_tensor"]),
+                                            "widen": round(float(last["prune_widen"]), 4)},
                                   "stage_ms": {k: round(last[k], 3) for k in
                                                ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles", "ms_recheck",
                                                 "ms_finalize")}}, n),
@@ -436,7 +438,8 @@ def run_secondary(args, world, rank, local):
         cfg.update({"units": int(units), "parallelism": "replicas" if world > 1 else "single-gpu",
                     "stage_ms": {k: round(last[k], 3) for k in ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles",
                                                                 "ms_recheck", "ms_finalize", "ms_total")},
-                    "tile_pairs": int(last["tile_pairs"]), "candidates": int(last["candidates"])})
+                    "tile_pairs": int(last["tile_pairs"]), "candidates": int(last["candidates"]),
+                    "prune": {"tensor_cores": bool(last["prune_tensor"]), "widen": round(float(last["prune_widen"]), 4)}})
         line = {"metric": SECONDARY[wl]["metric"], "value": value, "unit": SECONDARY[wl]["unit"], "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl == "k3" else "bf16",

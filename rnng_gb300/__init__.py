@@ -62,7 +62,7 @@ class Stats(ctypes.Structure):
                                                  "ms_prune", "ms_tiles", "ms_recheck", "ms_finalize", "ms_d2h")] + \
                [(k, ctypes.c_int64) for k in ("num_cells", "super_pairs", "tile_pairs", "tile_pairs_all", "pairs_evaluated",
                                               "candidates", "edges", "retries", "simplices", "kernel_launches")] + \
-               [("ms_gram", ctypes.c_double)]
+               [("ms_gram", ctypes.c_double), ("prune_widen", ctypes.c_double), ("prune_tensor", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -44,7 +44,7 @@ const int64_t* upload_i64(rnng_ctx* c, DevBuf& buf, const int64_t* v, int64_t co
 int64_t tiles_with_retry(rnng_ctx* c, Layout& L, int mode, EdgeOut& E)
 {
     unsigned long long cap = std::max<unsigned long long>(1u << 20, c->edge_cap_hint);
-    c->counters.reserve(sizeof(unsigned long long) * 8);
+    c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
     E.count = c->counters.as<unsigned long long>() + 4;
     for (int attempt = 0;; ++attempt) {
         c->edges_u.reserve(sizeof(uint32_t) * cap);
@@ -170,7 +170,8 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->edges_v, &c->edges_w, &c->out_u, &c->out_v, &c->out_w, &c->cub_tmp, &c->cand,
                           &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
                           &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
-                          &c->items, &c->items_tmp, &c->sched_tmp, &c->sym};
+                          &c->items, &c->items_tmp, &c->sched_tmp, &c->sym, &c->shift_buf, &c->ball_b16,
+                          &c->ball_info};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

@@ -487,6 +487,135 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
     }
 }
 
+// Level 2 on the tensor cores (d <= 256): one warp per surviving super pair computes the
+// 32 x 32 Gram block of the two super-tiles' BF16 ball centres with mma.sync (m16n8k16,
+// FP32 accumulation) and keeps a tile pair when one of its 4 x 4 ball pairs passes
+//
+//     n_a + n_b - 2 g  <=  (eps' + r_a + r_b + a_a + a_b)^2 + q_a + q_b   (+ relative slack)
+//
+// where n is the norm of the BF16 centre, a >= its distance to the shifted FP32 centre
+// and q its share of the tensor-core accumulation error (bf16_row), exactly the BF16
+// Gram candidate test with eps' widened by the two radii.  A pair with
+// |c_a - c_b| <= eps' + r_a + r_b therefore always passes, so no tile pair holding an
+// edge is dropped.  The k order inside each 32-column group is permuted identically
+// for both operands (a dot product does not depend on it) so that every lane fetches
+// its fragments with 16-byte loads: lane (g, t) reads columns 8t .. 8t + 7, which feed
+// k-slots {2t, 2t+1, 2t+8, 2t+9} of two consecutive k-steps.
+__device__ __forceinline__ void mma_bf16_16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+constexpr int kSB = kSuper * kBalls;  // balls per super-tile (32)
+
+__global__ void __launch_bounds__(256) k_tile_close_mma(const int2* __restrict__ supers,
+                                                        const unsigned long long* __restrict__ nsup_ptr,
+                                                        unsigned long long sup_cap, const uint4* __restrict__ cb,
+                                                        const float4* __restrict__ binfo, int dp, int64_t T,
+                                                        float eps_p, float kappa, int2* __restrict__ out,
+                                                        unsigned long long* __restrict__ count, unsigned long long cap)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const unsigned long long nsup = min(*nsup_ptr, sup_cap);
+    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    const int rowq = dp / 8;  // uint4 per BF16 row
+    for (unsigned long long w = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nsup; w += nw) {
+        const int2 sp = supers[w];
+        const int64_t ra = (int64_t)sp.x * kSB, rb = (int64_t)sp.y * kSB;  // first ball row of each side
+        float acc[2][4][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
+        const uint4* pa = cb + (ra + g) * rowq + t;
+        const uint4* pb = cb + (rb + g) * rowq + t;
+#pragma unroll 1
+        for (int kp = 0; kp < dp / 32; ++kp) {
+            uint4 a[2][2], b[4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) a[mt][h] = pa[(16 * mt + 8 * h) * rowq + 4 * kp];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) b[nt] = pb[(8 * nt) * rowq + 4 * kp];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    mma_bf16_16816(acc[mt][nt], a[mt][0].x, a[mt][1].x, a[mt][0].y, a[mt][1].y, b[nt].x, b[nt].y);
+                    mma_bf16_16816(acc[mt][nt], a[mt][0].z, a[mt][1].z, a[mt][0].w, a[mt][1].w, b[nt].z, b[nt].w);
+                }
+        }
+        // acc[mt][nt][2h + e] = ball row 16 mt + 8 h + g, ball column 8 nt + 2 t + e; their tiles
+        // are row tile 4 mt + 2 h + g / 4 and column tile 2 nt + t / 2 of the super pair
+        float4 ir[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ir[k] = binfo[ra + 8 * k + g];  // k = 2 mt + h
+        uint32_t msk = 0;  // bit 4 (2 mt + h) + nt
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const float4 y = binfo[rb + 8 * nt + 2 * t + e];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float4 x = ir[2 * mt + h];
+                        const float D = fmaf(-2.f, acc[mt][nt][2 * h + e], x.x + y.x);
+                        const float E = eps_p + x.w + y.w + x.y + y.y;
+                        const float R = fmaf(E, E, x.z + y.z);
+                        const bool keep = x.w >= 0.f && y.w >= 0.f && D <= R + kappa * (x.x + y.x + R);
+                        msk |= (keep ? 1u : 0u) << (4 * (2 * mt + h) + nt);
+                    }
+            }
+        // OR over the lanes holding the other balls of the same tiles (g % 4 and t % 2)
+        msk |= __shfl_xor_sync(0xffffffffu, msk, 1);
+        msk |= __shfl_xor_sync(0xffffffffu, msk, 4);
+        msk |= __shfl_xor_sync(0xffffffffu, msk, 8);
+        // lanes (g % 4 == 0, t % 2 == 0) report: row tiles g / 4 + 2 k, column tiles t / 2 + 2 nt
+        const bool reporter = (lane & 13) == 0;
+        uint32_t mine = 0;
+        if (reporter) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const int64_t i = (int64_t)sp.x * kSuper + (g >> 2) + 2 * k;
+                    const int64_t j = (int64_t)sp.y * kSuper + (t >> 1) + 2 * nt;
+                    if (((msk >> (4 * k + nt)) & 1u) && i < T && j < T && i <= j) mine |= 1u << (4 * k + nt);
+                }
+        }
+        const int cnt = __popc(mine);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total == 0) continue;
+        unsigned long long base = 0;
+        if (lane == 31) base = atomicAdd(count, (unsigned long long)total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        unsigned long long pos = base + (unsigned long long)(incl - cnt);
+        while (mine) {
+            const int bit = __ffs(mine) - 1;
+            mine &= mine - 1;
+            if (pos < cap)
+                out[pos] = make_int2(sp.x * kSuper + (g >> 2) + 2 * (bit >> 2), sp.y * kSuper + (t >> 1) + 2 * (bit & 3));
+            ++pos;
+        }
+    }
+}
+
 // Items of the persistent Gram kernel.  The pairs are sorted by (row tile, column
 // tile); inside a row they are grouped nt at a time into items {i, j0, j1} (j1 = -1 for
 // a row's last odd pair or nt = 1).  The items are cut into chunks of kSchedChunk and
@@ -579,7 +708,7 @@ void build_covers(rnng_ctx* c, Layout& L)
 void prune_covers(rnng_ctx* c, Layout& L)
 {
     cudaStream_t s = c->stream;
-    c->counters.reserve(sizeof(unsigned long long) * 8);
+    c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
     unsigned long long* cnt = c->counters.as<unsigned long long>();
     const double u = 5.9604644775390625e-08;
     const float eps_p = std::nextafter((float)((double)L.radius * (1.0 + (L.d + 8) * u) + 1e-30), INFINITY);
@@ -614,9 +743,34 @@ void prune_covers(rnng_ctx* c, Layout& L)
     RNNG_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), s));
     const unsigned grid = (unsigned)std::max<unsigned long long>(
         1, std::min<unsigned long long>((L.super_pairs + kSPB - 1) / kSPB, (unsigned long long)c->num_sms * 8));
-    k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
-                                      c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(), cnt + 1,
-                                      tile_cap); ++c->launches;
+    // Tensor-core ball Gram blocks (BF16 ball centres padded to S super-tiles of kSB rows)
+    // unless their error terms would widen the ball test by more than kMaxWiden on
+    // average: data whose extent is large against eps (then the FP32 kernel prunes more).
+    constexpr float kMaxWiden = 0.05f;
+    bool tc = bf16_supported(L.d);
+    const int dp = (int)ceil_div(L.d, 64) * 64;
+    if (tc) {
+        const int64_t nb = L.T * kBalls, nb_pad = L.S * kSB;
+        c->ball_b16.reserve(sizeof(__nv_bfloat16) * (size_t)nb_pad * dp);
+        c->ball_info.reserve(sizeof(float4) * (size_t)nb_pad);
+        const float widen = prepare_ball_bf16(c, L, c->tile_lo.as<float>(), c->tile_hi.as<float>(), nb, nb_pad, eps_p,
+                                              c->ball_b16.as<__nv_bfloat16>(), c->ball_info.as<float4>());
+        tc = widen <= kMaxWiden;
+        c->stats.prune_widen = widen;
+    }
+    c->stats.prune_tensor = tc ? 1 : 0;
+    if (tc) {
+        const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
+        const unsigned wgrid = (unsigned)std::max<unsigned long long>(
+            1, std::min<unsigned long long>((L.super_pairs + 7) / 8, (unsigned long long)c->num_sms * 8));
+        k_tile_close_mma<<<wgrid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->ball_b16.as<uint4>(),
+                                               c->ball_info.as<float4>(), dp, L.T, eps_p, kappa,
+                                               c->pair_list.as<int2>(), cnt + 1, tile_cap); ++c->launches;
+    } else {
+        k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
+                                          c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(),
+                                          cnt + 1, tile_cap); ++c->launches;
+    }
     unsigned long long got = 0;
     RNNG_CUDA(cudaMemcpyAsync(&got, cnt + 1, sizeof(got), cudaMemcpyDeviceToHost, s));
     RNNG_CUDA(cudaStreamSynchronize(s));

@@ -36,6 +36,11 @@ struct Error {
 
 // A growable device buffer owned by the context.  Buffers are reused across calls
 // so that steady-state calls do not allocate.
+// Slots of the context's 64-bit device counter array (counters): 0-1 pruning, 2-3 edit counts,
+// 4 edges, 5 candidates, 6 query hits, 9 edit maximum length, 10-11 rips checks,
+// 12 ball widening (two floats).
+constexpr int kCounterSlots = 16;
+
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -81,7 +86,7 @@ struct rnng_ctx {
     rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
         out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched, clq0, clq1,
-        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym;
+        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;
     int64_t last_candidates = 0;

@@ -636,7 +636,7 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             c->stats.tile_pairs_all = T * (T + 1) / 2;
             c->stats.pairs_evaluated = (int64_t)npairs * kET * kET;
             // 3. filter
-            c->counters.reserve(sizeof(unsigned long long) * 8);
+            c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
             unsigned long long* ccount = c->counters.as<unsigned long long>() + 2;
             unsigned long long* ecount = c->counters.as<unsigned long long>() + 3;
             unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
@@ -770,7 +770,7 @@ extern "C" int rnng_voronoi_edit(rnng_ctx* c, const uint8_t* atoms, const int64_
         const int64_t* dcoff = (const int64_t*)upload(c, c->aux7, coffsets, sizeof(int64_t) * (m + 1), flags);
         const uint8_t* dcatoms = (const uint8_t*)upload(c, c->pivots, catoms, (size_t)ncatoms, flags);
         // longest centre: sizes the shared match vectors and picks the register variant
-        c->counters.reserve(sizeof(unsigned long long) * 16);
+        c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
         unsigned long long* dmax = c->counters.as<unsigned long long>() + 9;
         RNNG_CUDA(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
         k_max_len<<<(unsigned)std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 4), 256, 0, s>>>(dcoff, m,

@@ -1,6 +1,7 @@
 // Internal interfaces of the L2 epsilon-graph pipeline (see eps_l2.cu).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 #include "common.cuh"
@@ -22,6 +23,7 @@ struct Layout {
     int64_t num_cells = 0;
     float radius = 0.f, relerr = 0.f;
     float* Xs = nullptr;          // n_pad x d, sorted by leaf cell, zero padded
+    const float* shift = nullptr;  // per-dimension shift of the BF16 operands (rounded column means)
     int32_t* perm = nullptr;      // sorted position -> input row
     unsigned long long super_pairs = 0, tile_pairs = 0;
     int2* pairs = nullptr;        // surviving tile pairs (i <= j)
@@ -58,6 +60,15 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
 
 // BF16 tensor-core Gram tiles with FP32 recheck (gram_bf16.cu).
 void prepare_bf16(rnng_ctx* c, Layout& L);
+// Relative bound gamma of the Gram error terms q = gamma ||x~||^2 for dimension d.
+double bf16_gamma(int d);
+// The BF16 shift of this layout (computed once per call; L.shift).
+const float* bf16_shift(rnng_ctx* c, Layout& L);
+// Ball centres (nb rows of L.d floats, radii rad; rows nb .. nb_pad - 1 padding) as BF16
+// rows of dp = 64 * ceil(d / 64) with {norm, a, q, radius or -1} per row (bf16_row).
+// Returns the mean relative widening of a ball pair's squared threshold by a and q.
+float prepare_ball_bf16(rnng_ctx* c, Layout& L, const float* cen, const float* rad, int64_t nb, int64_t nb_pad,
+                        float eps_p, __nv_bfloat16* out, float4* info);
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E);
 bool bf16_supported(int d);
 // Column tiles per Gram item for dimension d (2: N = 256 MMAs, 1: N = 128).

@@ -707,15 +707,26 @@ __global__ void __launch_bounds__(256) k_recheck(const float* __restrict__ Xs, i
 // ------------------------------------------------------------------------------------------------
 // BF16 operand preparation
 
-// Per-dimension column sums (double) of the real rows.
-__global__ void k_colsum(const float* __restrict__ Xs, int64_t n, int d, double* __restrict__ sums)
+// Per-dimension column sums (double) of the real rows, d <= 256: a block step covers
+// 256 / d whole rows as one contiguous run of floats, so thread t always adds dimension
+// t % d; per-thread float partials, then one double atomic per dimension and block.
+__global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, int64_t n, int d, double* __restrict__ sums)
 {
-    for (int k0 = 0; k0 < d; k0 += blockDim.x) {
-        const int k = k0 + threadIdx.x;
-        if (k >= d) continue;
-        double acc = 0.0;
-        for (int64_t r = blockIdx.x; r < n; r += gridDim.x) acc += (double)Xs[r * d + k];
-        atomicAdd(&sums[k], acc);
+    __shared__ float part[256];
+    const int rpb = 256 / d;  // rows per step
+    const int t = threadIdx.x;
+    const bool active = t < rpb * d;
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    float acc = 0.f;
+    if (active)
+        for (int64_t r = r0 + t / d; r < r1; r += rpb) acc += Xs[r * d + t % d];
+    part[t] = acc;
+    __syncthreads();
+    if (t < d) {
+        double s2 = 0.0;
+        for (int q = 0; q < rpb; ++q) s2 += (double)part[q * d + t];
+        if (r0 < r1) atomicAdd(&sums[t], s2);
     }
 }
 
@@ -724,45 +735,83 @@ __global__ void k_shift(const double* __restrict__ sums, int64_t n, int d, float
     for (int k = threadIdx.x; k < d; k += blockDim.x) shift[k] = (float)rint(sums[k] / (double)(n > 0 ? n : 1));
 }
 
+// One warp: the BF16 row of x (d floats; zeros when !real) shifted by `shift` and zero
+// padded to dp, written to out, and the row's {norm of the BF16 row, error radius a,
+// Gram error term q} in every lane.  a >= ||(x - shift) - bf16 row|| (the BF16 residual
+// plus the FP32 rounding of x - shift); q = gamma ||x~||^2, an upper bound on this
+// row's share of the FP32 error of a tensor-core Gram entry.
+__device__ __forceinline__ float3 bf16_row(const float* __restrict__ x, bool real, int d, int dp,
+                                           const float* __restrict__ shift, float gamma,
+                                           __nv_bfloat16* __restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const float u = 5.9604644775390625e-08f;  // 2^-24
+    float nrm = 0.f, res = 0.f, xc = 0.f;
+    for (int k = lane; k < dp; k += 32) {
+        float b = 0.f;
+        if (real && k < d) {
+            const float t = __fsub_rn(x[k], shift[k]);
+            const __nv_bfloat16 h = __float2bfloat16_rn(t);
+            b = __bfloat162float(h);
+            const float e = __fsub_rn(t, b);  // exact: b is t rounded to 8 bits
+            nrm = fmaf(b, b, nrm);
+            res = fmaf(e, e, res);
+            xc = fmaf(t, t, xc);
+        }
+        out[k] = __float2bfloat16_rn(b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+        res += __shfl_xor_sync(0xffffffffu, res, o);
+        xc += __shfl_xor_sync(0xffffffffu, xc, o);
+    }
+    const float grow = 1.f + (float)(d + 8) * u;
+    const float a = (sqrtf(res) + u * sqrtf(xc)) * grow * grow + 1e-30f;
+    const float q = gamma * nrm * grow;
+    return make_float3(nrm, a, q);
+}
+
 // One warp per sorted row: BF16 operand row (dp columns, zero padded) and the
-// row's {norm, error radius, Gram error term} for the candidate test.
+// row's {norm, error radius, Gram error term, norm - a^2 - q} for the candidate test.
 __global__ void k_to_bf16(const float* __restrict__ Xs, int64_t n, int64_t n_pad, int d, int dp,
                           const float* __restrict__ shift, float gamma, __nv_bfloat16* __restrict__ Xb,
                           float4* __restrict__ rowinfo)
 {
-    const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const float u = 5.9604644775390625e-08f;  // 2^-24
     for (int64_t r = warp; r < n_pad; r += nwarps) {
-        float nrm = 0.f, res = 0.f, xc = 0.f;
-        for (int k = lane; k < dp; k += 32) {
-            float b = 0.f;
-            if (r < n && k < d) {
-                const float t = __fsub_rn(Xs[r * d + k], shift[k]);
-                const __nv_bfloat16 h = __float2bfloat16_rn(t);
-                b = __bfloat162float(h);
-                const float e = __fsub_rn(t, b);  // exact: b is t rounded to 8 bits
-                nrm = fmaf(b, b, nrm);
-                res = fmaf(e, e, res);
-                xc = fmaf(t, t, xc);
+        const float3 v = bf16_row(Xs + r * d, r < n, d, dp, shift, gamma, Xb + r * dp);
+        if ((threadIdx.x & 31) == 0) rowinfo[r] = make_float4(v.x, v.y, v.z, v.x - v.y * v.y - v.z);
+    }
+}
+
+// One warp per ball: BF16 centre row and {norm, a, q, radius} (radius -1: no ball; its
+// row is zero).  Rows nb .. nb_pad - 1 are padding (no ball).  widen[0] accumulates, over
+// the balls, how much a and q widen a ball pair's squared threshold relative to
+// E = eps' + 2 r (the ball paired with itself), widen[1] the number of balls.
+__global__ void k_balls_bf16(const float* __restrict__ cen, const float* __restrict__ rad, int64_t nb, int64_t nb_pad,
+                             int d, int dp, const float* __restrict__ shift, float gamma, float eps_p,
+                             __nv_bfloat16* __restrict__ out, float4* __restrict__ info, float* __restrict__ widen)
+{
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float wsum = 0.f, wcnt = 0.f;
+    for (int64_t b = warp; b < nb_pad; b += nwarps) {
+        const float r = b < nb ? rad[b] : -1.f;
+        const float3 v = bf16_row(cen + b * d, r >= 0.f, d, dp, shift, gamma, out + b * dp);
+        if ((threadIdx.x & 31) == 0) {
+            info[b] = make_float4(v.x, v.y, v.z, r >= 0.f ? r : -1.f);
+            if (r >= 0.f) {
+                const float E = eps_p + 2.f * r, Ew = E + 2.f * v.y;
+                wsum += (Ew * Ew + 2.f * v.z) / fmaxf(E * E, 1e-30f) - 1.f;
+                wcnt += 1.f;
             }
-            Xb[r * dp + k] = __float2bfloat16_rn(b);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
-            res += __shfl_xor_sync(0xffffffffu, res, o);
-            xc += __shfl_xor_sync(0xffffffffu, xc, o);
-        }
-        if (lane == 0) {
-            const float grow = 1.f + (float)(d + 8) * u;
-            // a >= ||(x - c) - x~||: computed residual plus the FP32 rounding of x - c
-            const float a = (sqrtf(res) + u * sqrtf(xc)) * grow * grow + 1e-30f;
-            // q >= Gram error share of this row: gamma * ||x~||^2 (upper bound on the norm)
-            const float q = gamma * nrm * grow;
-            rowinfo[r] = make_float4(nrm, a, q, nrm - a * a - q);
-        }
+    }
+    if ((threadIdx.x & 31) == 0 && wcnt > 0.f) {
+        atomicAdd(&widen[0], wsum);
+        atomicAdd(&widen[1], wcnt);
     }
 }
 
@@ -813,6 +862,47 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode()
 
 bool bf16_supported(int d) { return d >= 1 && d <= kMaxDp; }
 
+double bf16_gamma(int d)
+{
+    // tensor-core accumulation is modelled as at most 2^-19 relative error per
+    // addition (truncating adds with fewer than 24 bits), far below its real error
+    const int dp = (int)ceil_div(d, kChunkK) * kChunkK;
+    return (double)dp * std::ldexp(1.0, -19) + (double)(d + 8) * std::ldexp(1.0, -24) + 2.0 * std::ldexp(1.0, -24);
+}
+
+const float* bf16_shift(rnng_ctx* c, Layout& L)
+{
+    if (L.shift) return L.shift;
+    cudaStream_t s = c->stream;
+    const int d = L.d;
+    c->shift_buf.reserve(sizeof(double) * d + sizeof(float) * d + 16);
+    double* sums = c->shift_buf.as<double>();
+    float* shift = (float*)(sums + d);
+    RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 4));
+    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(L.Xs, L.n, d, sums); ++c->launches;
+    k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
+    L.shift = shift;
+    return shift;
+}
+
+float prepare_ball_bf16(rnng_ctx* c, Layout& L, const float* cen, const float* rad, int64_t nb, int64_t nb_pad,
+                        float eps_p, __nv_bfloat16* out, float4* info)
+{
+    cudaStream_t s = c->stream;
+    const int dp = (int)ceil_div(L.d, kChunkK) * kChunkK;
+    const float* shift = bf16_shift(c, L);
+    float* widen = reinterpret_cast<float*>(c->counters.as<unsigned long long>() + 12);
+    RNNG_CUDA(cudaMemsetAsync(widen, 0, 2 * sizeof(float), s));
+    k_balls_bf16<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(nb_pad * 32, 256), (int64_t)c->num_sms * 16)),
+                   256, 0, s>>>(cen, rad, nb, nb_pad, L.d, dp, shift, (float)bf16_gamma(L.d), eps_p, out, info, widen);
+    ++c->launches;
+    float h[2] = {0.f, 0.f};
+    RNNG_CUDA(cudaMemcpyAsync(h, widen, sizeof(h), cudaMemcpyDeviceToHost, s));
+    RNNG_CUDA(cudaStreamSynchronize(s));
+    return h[1] > 0.f ? h[0] / h[1] : 0.f;
+}
+
 void prepare_bf16(rnng_ctx* c, Layout& L)
 {
     cudaStream_t s = c->stream;
@@ -820,22 +910,14 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     const int dp = (int)ceil_div(d, kChunkK) * kChunkK;
     c->xb_sorted.reserve(sizeof(__nv_bfloat16) * (size_t)L.n_pad * dp);
     c->norms.reserve(sizeof(float4) * (size_t)L.n_pad + sizeof(float) * (size_t)L.n_pad +
-                     sizeof(float2) * (size_t)L.T + sizeof(double) * d + sizeof(float) * d + 64);
+                     sizeof(float2) * (size_t)L.T + 64);
     float4* rowinfo = c->norms.as<float4>();
     float* ucol = (float*)(rowinfo + L.n_pad);
     float2* tileinfo = (float2*)(ucol + L.n_pad);
-    double* sums = (double*)(tileinfo + L.T + (L.T & 1));
-    float* shift = (float*)(sums + d);
-    RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
-    k_colsum<<<std::min<int64_t>(std::max<int64_t>(L.n / 256, 1), (int64_t)c->num_sms * 4), 128, 0, s>>>(L.Xs, L.n,
-                                                                                                           d, sums); ++c->launches;
-    k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
+    const float* shift = bf16_shift(c, L);
     const double u = std::ldexp(1.0, -24);
-    // tensor-core accumulation is modelled as at most 2^-19 relative error per
-    // addition (truncating adds with fewer than 24 bits), far below its real error
-    const double gamma = (double)dp * std::ldexp(1.0, -19) + (double)(d + 2) * u + 8.0 * u;
     k_to_bf16<<<std::min<int64_t>(ceil_div(L.n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0, s>>>(
-        L.Xs, L.n, L.n_pad, d, dp, shift, (float)gamma, c->xb_sorted.as<__nv_bfloat16>(), rowinfo); ++c->launches;
+        L.Xs, L.n, L.n_pad, d, dp, shift, (float)bf16_gamma(d), c->xb_sorted.as<__nv_bfloat16>(), rowinfo); ++c->launches;
     k_tile_info<<<(unsigned)L.T, kTile, 0, s>>>(rowinfo, L.T, ucol, tileinfo); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
     c->bf16_ucol = ucol;

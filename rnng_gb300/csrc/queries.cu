@@ -230,7 +230,7 @@ int rnng_radius_query_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_
         const float* dQ = (const float*)upload(c, c->x_sorted, Q, sizeof(float) * nq * d, flags);
         const int64_t* dQI = (const int64_t*)upload(c, c->aux7, qids, sizeof(int64_t) * nq, flags);
         unsigned long long cap = std::max<unsigned long long>(1u << 16, c->edge_cap_hint);
-        c->counters.reserve(sizeof(unsigned long long) * 8);
+        c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
         unsigned long long* cnt = c->counters.as<unsigned long long>() + 6;
         unsigned long long got = 0;
         if (n > 0 && nq > 0 && radius >= 0.f) {

@@ -728,7 +728,7 @@ void begin_call(rnng_ctx* c)
     c->stats = rnng_stats{};
     c->launches = 0;
     c->gram_ms = 0.0;
-    c->counters.reserve(sizeof(unsigned long long) * 16);
+    c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
     RNNG_CUDA(cudaEventRecord(c->ev[0], c->stream));
 }
 

@@ -296,6 +296,8 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     int32_t* cend = cstart + cap;
     int32_t* nchild = cend + cap;
     int32_t* child_off = nchild + cap;
+    // BF16 shift (d <= 256): the assignment's distances come from the tensor cores
+    const float* shift = bf16_supported(d) ? bf16_shift(c, L, dX) : nullptr;
     int levels = 0;
     for (; levels < kMaxLevels; ++levels) {
         k_cell_bounds<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(skeys, n, cstart, cend); ++c->launches;
@@ -314,7 +316,8 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         k_gather_rows<<<grid_for(c, (int64_t)total * d, 256), 256, 0, s>>>(dX, d, lm_idx, total, lm_rows); ++c->launches;
         // children ordered along a greedy nearest-neighbour chain of their landmarks
         chain_leaves(c, lm_rows, d, nchild, child_off, (int)ncells, c->aux5.as<int32_t>());
-        launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, c->aux5.as<int32_t>(), nkeys, nvals);
+        launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, c->aux5.as<int32_t>(), shift, nkeys,
+                      nvals);
         sort_pairs_u64(c, nkeys, skeys, nvals, order, n, 32 + bits_for(total));
         ncells = total;
     }

@@ -62,8 +62,9 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
 void prepare_bf16(rnng_ctx* c, Layout& L);
 // Relative bound gamma of the Gram error terms q = gamma ||x~||^2 for dimension d.
 double bf16_gamma(int d);
-// The BF16 shift of this layout (computed once per call; L.shift).
-const float* bf16_shift(rnng_ctx* c, Layout& L);
+// The BF16 shift of this layout: the rounded column means of the L.n points X (by
+// default L.Xs; the input rows give the same sums), computed once per call (L.shift).
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X = nullptr);
 // Ball centres (nb rows of L.d floats, radii rad; rows nb .. nb_pad - 1 padding) as BF16
 // rows of dp = 64 * ceil(d / 64) with {norm, a, q, radius or -1} per row (bf16_row).
 // Returns the mean relative widening of a ball pair's squared threshold by a and q.

@@ -870,9 +870,10 @@ double bf16_gamma(int d)
     return (double)dp * std::ldexp(1.0, -19) + (double)(d + 8) * std::ldexp(1.0, -24) + 2.0 * std::ldexp(1.0, -24);
 }
 
-const float* bf16_shift(rnng_ctx* c, Layout& L)
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X)
 {
     if (L.shift) return L.shift;
+    if (!X) X = L.Xs;
     cudaStream_t s = c->stream;
     const int d = L.d;
     c->shift_buf.reserve(sizeof(double) * d + sizeof(float) * d + 16);
@@ -880,7 +881,7 @@ const float* bf16_shift(rnng_ctx* c, Layout& L)
     float* shift = (float*)(sums + d);
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 4));
-    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(L.Xs, L.n, d, sums); ++c->launches;
+    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums); ++c->launches;
     k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
     L.shift = shift;
     return shift;

@@ -62,7 +62,8 @@ __device__ __forceinline__ void dist_block(DistSmem& sm, const float* __restrict
 
 
 // Nearest allowed column per row (see partition.cu); keys_out[row] = col << 32 | bits(dist).
+// With a BF16 shift (d <= 256) the distances come from the tensor cores.
 void launch_assign(rnng_ctx* c, const float* X, const int32_t* rowmap, int64_t nrows, int d, const float* C,
                    int64_t ncols, const uint64_t* row_key, const int32_t* cell_off, const int32_t* col_rank,
-                   uint64_t* keys_out, int32_t* vals_out);
+                   const float* shift, uint64_t* keys_out, int32_t* vals_out);
 }  // namespace rnng

@@ -272,15 +272,31 @@ __device__ void bisect(BisectState& st, const float* __restrict__ src, const flo
 }
 
 // One block per tile.  Output: centres [T][kBalls][d], radii [T][kBalls] (-1 = unused).
+// With staged = true the tile's rows are first copied to shared memory (kTile * d
+// floats of dynamic shared memory), which every pass of the bisection then reads.
 __global__ void __launch_bounds__(256) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d, float grow,
-                                                    float* __restrict__ cen, float* __restrict__ rad)
+                                                    bool staged, float* __restrict__ cen, float* __restrict__ rad)
 {
     __shared__ BisectState st;
+    extern __shared__ __align__(16) float tile_rows[];
     const int64_t t = blockIdx.x;
     const int64_t r0 = t * kTile;
     const int nitems = (int)min((int64_t)kTile, n - r0);
     float* mycen = cen + t * kBalls * d;
-    bisect(st, Xs + r0 * d, nullptr, nitems, d, mycen);
+    const float* src = Xs + r0 * d;
+    if (staged) {
+        const int total = nitems * d;
+        if ((d & 3) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* t4 = reinterpret_cast<float4*>(tile_rows);
+            for (int i = threadIdx.x; i < total / 4; i += blockDim.x) t4[i] = __ldg(s4 + i);
+        } else {
+            for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[i] = __ldg(src + i);
+        }
+        __syncthreads();
+        src = tile_rows;
+    }
+    bisect(st, src, nullptr, nitems, d, mycen);
     if (threadIdx.x < kBalls)
         rad[t * kBalls + threadIdx.x] = threadIdx.x < st.ngroups ? st.rad[threadIdx.x] * grow + 1e-30f : -1.f;
 }
@@ -698,7 +714,13 @@ void build_covers(rnng_ctx* c, Layout& L)
     c->super_lo.reserve(sizeof(float) * (size_t)L.S * kBalls * L.d);  // super ball centres
     c->super_hi.reserve(sizeof(float) * (size_t)L.S * kBalls);        // super ball radii
     c->pivots.reserve(sizeof(float) * (size_t)L.S * kSuper * kBalls * L.d);  // compaction workspace
-    k_tile_balls<<<(unsigned)L.T, 256, 0, s>>>(L.Xs, L.n, L.d, grow, c->tile_lo.as<float>(), c->tile_hi.as<float>()); ++c->launches;
+    // tiles staged in shared memory up to 64 dimensions (32 KB: the bisection's many block
+    // barriers need several blocks per SM, so larger tiles read through L1 instead)
+    const bool staged = L.d <= 64;
+    const size_t tsm = staged ? sizeof(float) * kTile * (size_t)L.d : 0;
+    if (staged) RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    k_tile_balls<<<(unsigned)L.T, 256, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, c->tile_lo.as<float>(),
+                                                 c->tile_hi.as<float>()); ++c->launches;
     k_super_balls<<<(unsigned)L.S, 256, 0, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d, grow,
                                                 c->pivots.as<float>(), c->super_lo.as<float>(),
                                                 c->super_hi.as<float>()); ++c->launches;

@@ -645,7 +645,9 @@ __global__ void __maxnreg__(kGramMaxRegs)
 // ------------------------------------------------------------------------------------------------
 // exact recheck of the candidates with the reference's sequential FP32 L2
 
-__global__ void __launch_bounds__(256) k_recheck(const float* __restrict__ Xs, int d, const uint2* __restrict__ cand,
+// Exact recheck, any d: one candidate per thread reading its two rows directly (short
+// rows are a few cache lines each).
+__global__ void __launch_bounds__(256) k_recheck_direct(const float* __restrict__ Xs, int d, const uint2* __restrict__ cand,
                                                  const unsigned long long* __restrict__ ncand_ptr,
                                                  unsigned long long cand_cap, float radius, uint32_t* __restrict__ eu,
                                                  uint32_t* __restrict__ ev, float* __restrict__ ew,
@@ -690,6 +692,93 @@ __global__ void __launch_bounds__(256) k_recheck(const float* __restrict__ Xs, i
             int acc = 0;
             for (int k = 0; k < 8; ++k) { int t = s_warp[k]; s_warp[k] = acc; acc += t; }
             s_base = acc ? atomicAdd(ecount, (unsigned long long)acc) : 0ull;
+        }
+        __syncthreads();
+        if (hit) {
+            const unsigned long long pos = s_base + s_warp[warp] + __popc(ball & ((1u << lane) - 1u));
+            if (pos < cap) {
+                eu[pos] = c.x;
+                ev[pos] = c.y;
+                ew[pos] = w;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Exact recheck for d a multiple of 32 (k_recheck_direct otherwise).
+// One candidate per thread, summed in RNNG's order (dimension 0, 1, ...).  A warp's 32
+// candidates read their two rows through shared memory, 32 dimensions at a time: the
+// warp loads the 32 rows' slices together (coalesced, many loads in flight) and stores
+// them transposed, slice[k][j] with rows padded to 33 floats, so that the per-thread
+// reads (fixed k, j = lane) hit 32 distinct banks.
+constexpr int kRecheckWarps = 4;
+
+__global__ void __launch_bounds__(32 * kRecheckWarps) k_recheck(const float* __restrict__ Xs, int d,
+                                                                const uint2* __restrict__ cand,
+                                                                const unsigned long long* __restrict__ ncand_ptr,
+                                                                unsigned long long cand_cap, float radius,
+                                                                uint32_t* __restrict__ eu, uint32_t* __restrict__ ev,
+                                                                float* __restrict__ ew,
+                                                                unsigned long long* __restrict__ ecount,
+                                                                unsigned long long cap)
+{
+    __shared__ float slice[kRecheckWarps][2][32][33];
+    __shared__ int64_t rowp[kRecheckWarps][2][32];
+    __shared__ int s_warp[kRecheckWarps];
+    __shared__ unsigned long long s_base;
+    const unsigned long long nc = min(*ncand_ptr, cand_cap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float(*sp)[33] = slice[warp][0];
+    float(*sq)[33] = slice[warp][1];
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    // iterate in block-uniform rounds so that the block-level append stays collective
+    for (unsigned long long round = (unsigned long long)blockIdx.x * blockDim.x; round < nc; round += stride) {
+        const unsigned long long e = round + threadIdx.x;
+        const bool valid = e < nc;
+        const uint2 c = valid ? cand[e] : make_uint2(0, 0);
+        rowp[warp][0][lane] = valid ? (int64_t)c.y * d : -1;
+        rowp[warp][1][lane] = valid ? (int64_t)c.x * d : -1;
+        float acc = 0.f;
+        for (int k0 = 0; k0 < d; k0 += 32) {
+            __syncwarp();
+            {
+                // 16-byte loads: lane l takes dimensions k0 + 4 (l % 8) .. + 3 of rows j0 + l / 8;
+                // all 16 loads are independent, and (4 (l % 8) + i) * 33 + j0 + l / 8 keeps the
+                // transposed stores in distinct banks
+                const int kq = 4 * (lane & 7), jr = lane >> 3;
+                float4 vp[8], vq[8];
+#pragma unroll
+                for (int j0 = 0; j0 < 8; ++j0) {
+                    const int64_t pr = rowp[warp][0][4 * j0 + jr], qr = rowp[warp][1][4 * j0 + jr];
+                    vp[j0] = pr >= 0 ? __ldg(reinterpret_cast<const float4*>(Xs + pr + k0 + kq)) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    vq[j0] = pr >= 0 ? __ldg(reinterpret_cast<const float4*>(Xs + qr + k0 + kq)) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int j0 = 0; j0 < 8; ++j0) {
+                    const int j = 4 * j0 + jr;
+                    sp[kq + 0][j] = vp[j0].x; sp[kq + 1][j] = vp[j0].y; sp[kq + 2][j] = vp[j0].z; sp[kq + 3][j] = vp[j0].w;
+                    sq[kq + 0][j] = vq[j0].x; sq[kq + 1][j] = vq[j0].y; sq[kq + 2][j] = vq[j0].z; sq[kq + 3][j] = vq[j0].w;
+                }
+            }
+            __syncwarp();
+            if (valid)
+#pragma unroll 8
+                for (int k = 0; k < 32; ++k) acc = l2seq_acc(acc, sp[k][lane], sq[k][lane]);
+        }
+        float w = 0.f;
+        bool hit = false;
+        if (valid) {
+            w = __fsqrt_rn(acc);
+            hit = (w <= radius);
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) s_warp[warp] = __popc(ball);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int a = 0;
+            for (int k = 0; k < kRecheckWarps; ++k) { const int t = s_warp[k]; s_warp[k] = a; a += t; }
+            s_base = a ? atomicAdd(ecount, (unsigned long long)a) : 0ull;
         }
         __syncthreads();
         if (hit) {
@@ -1027,10 +1116,18 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     }
     RNNG_CUDA(cudaEventRecord(c->ev[8], s));
     const unsigned long long ncand = (unsigned long long)c->last_candidates;
+    const int rthreads = 32 * kRecheckWarps;
     const int rgrid = (int)std::max<unsigned long long>(
-        1, std::min<unsigned long long>((ncand + 255) / 256, (unsigned long long)c->num_sms * 8));
-    k_recheck<<<rgrid, 256, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w, E.count,
-                                    E.cap); ++c->launches;
+        1, std::min<unsigned long long>((ncand + rthreads - 1) / rthreads, (unsigned long long)c->num_sms * 16));
+    if ((L.d & 31) == 0)
+        k_recheck<<<rgrid, rthreads, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w,
+                                             E.count, E.cap);
+    else
+        k_recheck_direct<<<(int)std::max<unsigned long long>(
+                               1, std::min<unsigned long long>((ncand + 255) / 256, (unsigned long long)c->num_sms * 8)),
+                           256, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w, E.count,
+                                        E.cap);
+    ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 

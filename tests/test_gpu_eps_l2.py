@@ -95,3 +95,22 @@ def test_modes_agree_and_fp64_error(ctx):
     u, v, w = a
     d64 = np.sqrt(((x[u].astype(np.float64) - x[v].astype(np.float64)) ** 2).sum(1))
     assert np.max(np.abs(w - d64)) < 1e-5 * max(1.0, float(r))
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_both_pruning_paths_exact(ctx, orc, mode):
+    """Tile pairs are pruned on the tensor cores when the BF16 ball test is tight (compact
+    integer descriptors) and by the FP32 ball test when its error terms would widen it
+    (tight clusters whose spread is large against eps); both keep every edge."""
+    from rnng_gb300 import synth
+    rng = np.random.default_rng(32)
+    far = rng.normal(size=(40, 16))
+    far = 1000.0 * far / np.linalg.norm(far, axis=1, keepdims=True)  # tight clusters on a sphere of radius 1000
+    spread = (far[rng.integers(0, 40, 8000)] + 0.1 * rng.normal(size=(8000, 16))).astype(np.float32)
+    cases = [(synth.descriptor(n=20000, d=128, k=20, seed=31), synth.EPS_K2, 1),
+             (spread, np.float32(0.45), 0)]
+    for x, r, tensor in cases:
+        got = ctx.eps_graph_l2(x, r, mode=mode)
+        st = ctx.stats()
+        assert st["prune_tensor"] == tensor, st["prune_widen"]
+        assert same(got, orc.eps_graph_l2(x, r)) and got[0].size > 0

@@ -112,29 +112,55 @@ struct BisectState {
     int count[kBalls];
     int ngroups;
     int a, b;
-    float red_v[256];
-    int red_i[256];
+    float red_v[65];
+    int red_i[66];
+    float part[256];  // centroid partial sums (blockDim <= 256)
+    int pcnt[256];
 };
 
-// block-wide (max value, index) reduction; ties -> smaller index
-__device__ void block_argmax(BisectState& st, float v, int i, float& out_v, int& out_i)
+// (max value, index) of a pair (ties -> smaller index), and a count summed alongside
+__device__ __forceinline__ void argmax_step(float& v, int& i, int& n, float ov, int oi, int on)
 {
-    st.red_v[threadIdx.x] = v;
-    st.red_i[threadIdx.x] = i;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            const float ov = st.red_v[threadIdx.x + o];
-            const int oi = st.red_i[threadIdx.x + o];
-            if (ov > st.red_v[threadIdx.x] || (ov == st.red_v[threadIdx.x] && oi < st.red_i[threadIdx.x])) {
-                st.red_v[threadIdx.x] = ov;
-                st.red_i[threadIdx.x] = oi;
-            }
-        }
-        __syncthreads();
+    if (ov > v || (ov == v && oi < i)) {
+        v = ov;
+        i = oi;
     }
-    out_v = st.red_v[0];
-    out_i = st.red_i[0];
+    n += on;
+}
+
+// block-wide (max value, index) reduction with ties -> smaller index, plus the sum of
+// `cnt`: warp shuffles, then one warp over the per-warp results (two block barriers)
+__device__ void block_argmax(BisectState& st, float v, int i, float& out_v, int& out_i, int cnt, int* out_cnt)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        argmax_step(v, i, cnt, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o),
+                    __shfl_xor_sync(0xffffffffu, cnt, o));
+    if (lane == 0) {
+        st.red_v[warp] = v;
+        st.red_i[warp] = i;
+        st.red_i[32 + warp] = cnt;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        float wv = lane < nw ? st.red_v[lane] : -INFINITY;
+        int wi = lane < nw ? st.red_i[lane] : -1;
+        int wn = lane < nw ? st.red_i[32 + lane] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            argmax_step(wv, wi, wn, __shfl_xor_sync(0xffffffffu, wv, o), __shfl_xor_sync(0xffffffffu, wi, o),
+                        __shfl_xor_sync(0xffffffffu, wn, o));
+        if (lane == 0) {
+            st.red_v[64] = wv;
+            st.red_i[64] = wi;
+            st.red_i[65] = wn;
+        }
+    }
+    __syncthreads();
+    out_v = st.red_v[64];
+    out_i = st.red_i[64];
+    if (out_cnt) *out_cnt = st.red_i[65];
     __syncthreads();
 }
 
@@ -152,10 +178,39 @@ __device__ __forceinline__ float warp_dist(const float* __restrict__ x, const fl
     return sqrtf(s);
 }
 
-// centroid of group g into cen (d floats, global scratch owned by the block)
+// centroid of group g into cen (d floats, global scratch owned by the block): for
+// d <= blockDim / 2 the items are split over blockDim / d thread groups (thread t adds
+// dimension t % d of items t / d, t / d + H, ...) and the partial sums combined in
+// shared memory; any summation order gives a valid centre (radii are measured from it)
 __device__ void group_centroid(BisectState& st, const float* __restrict__ src, int nitems, int d, int g,
                                float* __restrict__ cen)
 {
+    const int H = d <= (int)blockDim.x / 2 ? (int)blockDim.x / d : 1;
+    if (H > 1) {
+        const int k = threadIdx.x % d, h = threadIdx.x / d;
+        float s = 0.f;
+        int cnt = 0;
+        if (h < H)
+            for (int r = h; r < nitems; r += H)
+                if (st.label[r] == g) {
+                    s += src[(int64_t)r * d + k];
+                    ++cnt;
+                }
+        st.part[threadIdx.x] = s;
+        st.pcnt[threadIdx.x] = cnt;
+        __syncthreads();
+        if ((int)threadIdx.x < d) {
+            float t = 0.f;
+            int c = 0;
+            for (int q = 0; q < H; ++q) {
+                t += st.part[q * d + k];
+                c += st.pcnt[q * d + k];
+            }
+            cen[k] = c ? t / (float)c : 0.f;
+        }
+        __syncthreads();
+        return;
+    }
     for (int k = threadIdx.x; k < d; k += blockDim.x) {
         float s = 0.f;
         int cnt = 0;
@@ -188,19 +243,12 @@ __device__ void group_radius(BisectState& st, const float* __restrict__ src, con
             if (st.dist[r] > best) { best = st.dist[r]; bi = r; }
         }
     float v;
-    int i;
-    block_argmax(st, best, bi, v, i);
-    // counts via a second reduction on the same buffers
-    st.red_i[threadIdx.x] = cnt;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) st.red_i[threadIdx.x] += st.red_i[threadIdx.x + o];
-        __syncthreads();
-    }
+    int i, total;
+    block_argmax(st, best, bi, v, i, cnt, &total);
     if (threadIdx.x == 0) {
         st.rad[g] = v;
         st.far_idx[g] = i;
-        st.count[g] = st.red_i[0];
+        st.count[g] = total;
     }
     __syncthreads();
 }
@@ -236,7 +284,7 @@ __device__ void bisect(BisectState& st, const float* __restrict__ src, const flo
             if (st.label[r] == g && st.dist[r] > best) { best = st.dist[r]; bi = r; }
         float v;
         int b;
-        block_argmax(st, best, bi, v, b);
+        block_argmax(st, best, bi, v, b, 0, nullptr);
         if (b < 0 || b == a || v <= 0.f) {
             // nothing to split: mark the group unsplittable
             if (threadIdx.x == 0) st.count[g] = 1;

@@ -221,6 +221,14 @@ __device__ __forceinline__ void tmem_ld16x256b_x8(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Three-input maximum (exact, like fmaxf(fmaxf(a, b), c)).
+__device__ __forceinline__ float max3f(float a, float b, float c)
+{
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Three-input minimum (exact, like fminf(fminf(a, b), c)).
 __device__ __forceinline__ float min3f(float a, float b, float c)
 {
@@ -294,9 +302,13 @@ struct ItemPrefetch {
 // stays resident while its row lasts and all CTAs work on neighbouring rows at the
 // same time (B tiles are shared through L2).
 
-template <int KCH, int NT>  // KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item
+// KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item; FOLD: the column
+// tiles come from tmapB with the column terms folded into their padding (k_to_bf16), so
+// the accumulator already holds g - u_j / 2 and the test needs no u_j
+template <int KCH, int NT, bool FOLD>
 __global__ void __maxnreg__(kGramMaxRegs)
-    k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const int4* __restrict__ items, unsigned long long nitems,
+    k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmapB,
+                const int4* __restrict__ items, unsigned long long nitems,
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
                 unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
@@ -354,6 +366,8 @@ __global__ void __maxnreg__(kGramMaxRegs)
         if (lane == 0) {
             // ---------------- TMA producer
             asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmap) : "memory");
+            if (FOLD) asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmapB) : "memory");
+            const CUtensorMap* bmap = FOLD ? &tmapB : &tmap;
             uint32_t aloads = 0;
             int cur_i = -1;
             uint32_t issued = 0, last_phase = 0;  // per ring slot: loads issued, phase of the last
@@ -381,9 +395,9 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 // stacked rows of one 128 NT-row operand
 #pragma unroll
                 for (int kc = 0; kc < KCH; ++kc) {
-                    tma_load_2d(slot + (kc * NT) * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, it.y * kTile);
+                    tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkK, it.y * kTile);
                     if (second)
-                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, &tmap, &b_full[q], kc * kChunkK, it.z * kTile);
+                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkK, it.z * kTile);
                 }
                 issued |= 1u << q;
                 last_phase = (last_phase & ~(1u << q)) | (ph << q);
@@ -498,7 +512,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
         float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
         float2 tj = make_float2(0.f, 0.f);
         if (ubeg < wend && it_j >= 0) {
-            uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
+            if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
             ri = rowinfo[(int64_t)it_i * kTile + r];
             tj = tileinfo[it_j];
         }
@@ -519,7 +533,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
             const bool diag = it_i == jt;
             // staged for the fragment threads: column 8 m + 2 q + e at float 20 q + 2 m + e, so that
             // thread (., q) reads its 16 terms as four 16-byte loads, the four q rows in distinct banks
-            reinterpret_cast<float2*>(colu)[(lane & 3) * 10 + (lane >> 2)] = uc;
+            if (!FOLD) reinterpret_cast<float2*>(colu)[(lane & 3) * 10 + (lane >> 2)] = uc;
             float Wk[4];
             {
                 const float A = eps_p + ri.y;
@@ -534,7 +548,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 it_i = itn.x;
                 it_j = half ? itn.z : itn.y;
                 if (w + ustride < wend && it_j >= 0) {
-                    uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
+                    if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
                     ri = rowinfo[(int64_t)it_i * kTile + r];
                     tj = tileinfo[it_j];
                 }
@@ -562,7 +576,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
             float2 u2[8];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                const float4 v = reinterpret_cast<const float4*>(colu + 20 * q4)[t];
+                const float4 v = FOLD ? make_float4(0.f, 0.f, 0.f, 0.f) : reinterpret_cast<const float4*>(colu + 20 * q4)[t];
                 u2[2 * t] = make_float2(v.x, v.y);
                 u2[2 * t + 1] = make_float2(v.z, v.w);
             }
@@ -578,21 +592,39 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[b]);
                 }
-                // most rows have no candidate: test each row's minimum first.  Packed pairs:
-                // __ffma2_rn forms two terms -2 g + u_j, each rounded once as fmaf; a
-                // three-input minimum takes both into one of the row's two running minima.
-                float mk[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
-                const float2 k2 = make_float2(-2.f, -2.f);
+                // most rows have no candidate: test each row's minimum term first
+                float mk[4];
+                if constexpr (FOLD) {
+                    // g holds g - u_j / 2, so the term -2 g + u_j is -2 g (exact): keep each row's
+                    // maximum of g (three-input maxima) and scale it once
 #pragma unroll
-                for (int m = 0; m < 8; ++m)
+                    for (int q = 0; q < 4; ++q) mk[q] = -INFINITY;
 #pragma unroll
-                    for (int hi = 0; hi < 2; ++hi) {
-                        const int x = 4 * m + 2 * hi;
-                        const float2 p = __ffma2_rn(make_float2(g[x], g[x + 1]), k2, u2[m]);
-                        g[x] = p.x;  // g now holds the terms
-                        g[x + 1] = p.y;
-                        mk[2 * hi + (m & 1)] = min3f(mk[2 * hi + (m & 1)], p.x, p.y);
-                    }
+                    for (int m = 0; m < 8; ++m)
+#pragma unroll
+                        for (int hi = 0; hi < 2; ++hi) {
+                            const int x = 4 * m + 2 * hi;
+                            mk[2 * hi + (m & 1)] = max3f(mk[2 * hi + (m & 1)], g[x], g[x + 1]);
+                        }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) mk[q] *= -2.f;
+                } else {
+                    // packed pairs: __ffma2_rn forms two terms -2 g + u_j, each rounded once as
+                    // fmaf; a three-input minimum takes both into one of the row's running minima
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) mk[q] = INFINITY;
+                    const float2 k2 = make_float2(-2.f, -2.f);
+#pragma unroll
+                    for (int m = 0; m < 8; ++m)
+#pragma unroll
+                        for (int hi = 0; hi < 2; ++hi) {
+                            const int x = 4 * m + 2 * hi;
+                            const float2 p = __ffma2_rn(make_float2(g[x], g[x + 1]), k2, u2[m]);
+                            g[x] = p.x;  // g now holds the terms
+                            g[x + 1] = p.y;
+                            mk[2 * hi + (m & 1)] = min3f(mk[2 * hi + (m & 1)], p.x, p.y);
+                        }
+                }
                 const float W0 = Wk[2 * hh], W1 = Wk[2 * hh + 1];
                 const bool mine = fminf(mk[0], mk[1]) <= W0 || fminf(mk[2], mk[3]) <= W1;
                 if (!__any_sync(0xffffffffu, mine)) continue;
@@ -604,7 +636,8 @@ __global__ void __maxnreg__(kGramMaxRegs)
                         const int gi = r0 + 8 * ((x >> 1) & 1);
                         const int gj = cb + 8 * (x >> 2) + (x & 1);
                         // padding rows / columns and, inside a diagonal tile, j <= i excluded
-                        const bool ok = g[x] <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
+                        const float term = FOLD ? -2.f * g[x] : g[x];
+                        const bool ok = term <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
                         msk |= (ok ? 1u : 0u) << x;
                     }
                 }
@@ -863,15 +896,42 @@ __device__ __forceinline__ float3 bf16_row(const float* __restrict__ x, bool rea
 
 // One warp per sorted row: BF16 operand row (dp columns, zero padded) and the
 // row's {norm, error radius, Gram error term, norm - a^2 - q} for the candidate test.
+// With fold (dp >= d + 4) the row is written twice: as a row-tile operand (Xb) with
+// 1 in columns d .. d + 3, and as a column-tile operand (XbB) with -v there, v = u/2
+// split exactly into four BF16 terms, u = n - a^2 - q - 2 gamma (n + a^2 + q).  A
+// tensor-core Gram entry of the two is then g - u_j / 2 directly: the folded column
+// term rides in the accumulation, whose error bound grows by gamma |u|, which the
+// extra 2 gamma (n + a^2 + q) in u absorbs, so the candidate test -2 g' <= W_i keeps
+// exactly the guarantee of -2 g + u_j <= W_i.
 __global__ void k_to_bf16(const float* __restrict__ Xs, int64_t n, int64_t n_pad, int d, int dp,
                           const float* __restrict__ shift, float gamma, __nv_bfloat16* __restrict__ Xb,
-                          float4* __restrict__ rowinfo)
+                          float4* __restrict__ rowinfo, bool fold, __nv_bfloat16* __restrict__ XbB)
 {
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
     for (int64_t r = warp; r < n_pad; r += nwarps) {
         const float3 v = bf16_row(Xs + r * d, r < n, d, dp, shift, gamma, Xb + r * dp);
-        if ((threadIdx.x & 31) == 0) rowinfo[r] = make_float4(v.x, v.y, v.z, v.x - v.y * v.y - v.z);
+        if (fold) {
+            // the same row as a column-tile operand (padding written below)
+            for (int k = lane; k < d; k += 32) XbB[r * dp + k] = Xb[r * dp + k];
+            for (int k = d + 4 + lane; k < dp; k += 32) XbB[r * dp + k] = __float2bfloat16_rn(0.f);
+        }
+        __syncwarp();  // the zeros other lanes wrote to columns d .. d + 3 come first
+        if (lane == 0) {
+            rowinfo[r] = make_float4(v.x, v.y, v.z, v.x - v.y * v.y - v.z);
+            if (fold) {
+                const float big = v.x + v.y * v.y + v.z;
+                float rest = 0.5f * (v.x - v.y * v.y - v.z - 2.f * gamma * big);
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const __nv_bfloat16 h = __float2bfloat16_rn(rest);
+                    rest = __fsub_rn(rest, __bfloat162float(h));  // exact
+                    Xb[r * dp + d + t] = __float2bfloat16_rn(1.f);
+                    XbB[r * dp + d + t] = __hneg(h);
+                }
+            }
+        }
     }
 }
 
@@ -1006,8 +1066,12 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     float2* tileinfo = (float2*)(ucol + L.n_pad);
     const float* shift = bf16_shift(c, L);
     const double u = std::ldexp(1.0, -24);
+    // four free padding columns carry the column terms through the tensor cores
+    c->bf16_fold = dp - d >= 4;
+    if (c->bf16_fold) c->xb_sortedB.reserve(sizeof(__nv_bfloat16) * (size_t)L.n_pad * dp);
     k_to_bf16<<<std::min<int64_t>(ceil_div(L.n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0, s>>>(
-        L.Xs, L.n, L.n_pad, d, dp, shift, (float)bf16_gamma(d), c->xb_sorted.as<__nv_bfloat16>(), rowinfo); ++c->launches;
+        L.Xs, L.n, L.n_pad, d, dp, shift, (float)bf16_gamma(d), c->xb_sorted.as<__nv_bfloat16>(), rowinfo,
+        c->bf16_fold, c->bf16_fold ? c->xb_sortedB.as<__nv_bfloat16>() : nullptr); ++c->launches;
     k_tile_info<<<(unsigned)L.T, kTile, 0, s>>>(rowinfo, L.T, ucol, tileinfo); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
     c->bf16_ucol = ucol;
@@ -1028,37 +1092,51 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    CUtensorMap& tmb = *reinterpret_cast<CUtensorMap*>(c->tmapB);
+    r = get_encode()(&tmb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, c->bf16_fold ? c->xb_sortedB.ptr : c->xb_sorted.ptr,
+                     gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int KCH, int NT>
-static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, const CUtensorMap& tm, const int4* items,
+template <int KCH, int NT, bool FOLD>
+static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, const CUtensorMap& tm,
+                          const CUtensorMap& tmb, const int4* items,
                           unsigned long long nitems, const float4* rowinfo, const float* ucol, const float2* tileinfo,
                           int64_t n, float eps_p, float kappa, uint2* cand, unsigned long long* cnt,
                           unsigned long long ccap, const unsigned long long* sched, int* fault)
 {
     if (!launch) {
-        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
         return;
     }
-    k_gram_bf16<KCH, NT><<<grid, kGramThreads, smem, s>>>(tm, items, nitems, rowinfo, ucol, tileinfo, n, eps_p, kappa,
-                                                          cand, cnt, ccap, sched, fault);
+    k_gram_bf16<KCH, NT, FOLD><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
+                                                                eps_p, kappa, cand, cnt, ccap, sched, fault);
 }
 
-// Sets the shared-memory size (launch = false) or launches the instance for (kch, nt).
-template <class... Args>
-static void gram_dispatch(int kch, int nt, Args... args)
+// Sets the shared-memory size (launch = false) or launches the instance for (kch, nt, fold).
+template <bool FOLD, class... Args>
+static void gram_dispatch_fold(int kch, int nt, Args... args)
 {
     if (nt == 2) {
-        if (kch == 1) gram_instance<1, 2>(args...);
-        else gram_instance<2, 2>(args...);
+        if (kch == 1) gram_instance<1, 2, FOLD>(args...);
+        else gram_instance<2, 2, FOLD>(args...);
     } else {
         switch (kch) {
-            case 1: gram_instance<1, 1>(args...); break;
-            case 2: gram_instance<2, 1>(args...); break;
-            case 3: gram_instance<3, 1>(args...); break;
-            default: gram_instance<4, 1>(args...); break;
+            case 1: gram_instance<1, 1, FOLD>(args...); break;
+            case 2: gram_instance<2, 1, FOLD>(args...); break;
+            case 3: gram_instance<3, 1, FOLD>(args...); break;
+            default: gram_instance<4, 1, FOLD>(args...); break;
         }
     }
+}
+
+template <class... Args>
+static void gram_dispatch(bool fold, int kch, int nt, Args... args)
+{
+    if (fold) gram_dispatch_fold<true>(kch, nt, args...);
+    else gram_dispatch_fold<false>(kch, nt, args...);
 }
 
 int gram_item_tiles(int d)
@@ -1081,8 +1159,10 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     const float4* rowinfo = (const float4*)c->bf16_rowinfo;
     const float* ucol = (const float*)c->bf16_ucol;
     const float2* tileinfo = (const float2*)c->bf16_tileinfo;
-    gram_dispatch(kchunks, nt, false, 0, smem, s, tm, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n, c->bf16_eps_p,
-                  0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
+    const CUtensorMap& tmb = *reinterpret_cast<const CUtensorMap*>(c->tmapB);
+    const bool fold = c->bf16_fold;
+    gram_dispatch(fold, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n,
+                  c->bf16_eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
     const int grid = L.sched_G;
     RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
     const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
@@ -1090,8 +1170,8 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
-        gram_dispatch(kchunks, nt, true, grid, smem, s, tm, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n,
-                      c->bf16_eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+        gram_dispatch(fold, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
+                      L.n, c->bf16_eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
         ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));

@@ -19,6 +19,7 @@
 #include <cfloat>
 #include <cstring>
 
+#include "balls.cuh"
 #include "common.cuh"
 #include "eps_l2.cuh"
 #include "kernels_misc.cuh"
@@ -99,102 +100,49 @@ __global__ void k_edit_emit_pairs(const int32_t* __restrict__ cnt, const int32_t
         for (int k = threadIdx.x; k < cnt[i]; k += blockDim.x) pairs[off[i] + k] = make_int2((int)i, (int)(i + k));
 }
 
-// Filter: length and profile L1 tests for all pairs of each tile pair; survivors are
-// appended as (sorted index a, sorted index b), a < b.  The profile L1 sums are a small
-// integer GEMM: thread (ty, tx) keeps the 8 x 8 block of rows ty*8.. and columns tx*8..,
-// and for every profile word loads 8 words of each side (two 16-byte loads per side from
-// the word-major shared copy) for 64 __vsadu4; the length test masks the block afterwards.
-__global__ void __launch_bounds__(256) k_edit_filter(const uint32_t* __restrict__ prof,
-                                                     const uint32_t* __restrict__ slen, int64_t n,
-                                                     const int2* __restrict__ pairs, int64_t npairs, int K,
-                                                     uint2* __restrict__ cand, unsigned long long* __restrict__ ccount,
-                                                     unsigned long long cap)
+// Filter operand: the profile thermometer-coded with counts capped at 8, one warp per
+// row, bin b's levels l = 0..7 at byte 8 b + l (E4M3 1.0 = 0x38 when count > l, else 0).
+// Then x_a . x_b = sum over bins of min(min(c_a, 8), min(c_b, 8)) and with n = sum of
+// min(c, 8), n_a + n_b - 2 x_a.x_b is the L1 distance of the capped profiles: never
+// above the L1 of the counts themselves, so it is still <= 2 q K for strings within K.
+// rowinfo = {n, 0, 0, n} and ucol = n are the tensor-core kernel's row and column terms.
+__global__ void k_edit_thermo(const uint32_t* __restrict__ prof, int64_t n_pad, uint8_t* __restrict__ x8,
+                              float4* __restrict__ rowinfo, float* __restrict__ ucol)
 {
-    constexpr int kW = kBins / 4;  // profile words per string
-    __shared__ __align__(16) uint32_t pa[kW][kET], pb[kW][kET];
-    __shared__ uint32_t la[kET], lb[kET];
-    __shared__ int s_warp[8];
-    __shared__ unsigned long long s_base;
-    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15, lane = tid & 31, warp = tid >> 5;
-    const uint32_t thr = (uint32_t)(2 * kQ * K);
-    for (int64_t w = blockIdx.x; w < npairs; w += gridDim.x) {
-        const int2 tp = pairs[w];
-        const int64_t i0 = (int64_t)tp.x * kET, j0 = (int64_t)tp.y * kET;
-        __syncthreads();
-        // coalesced 16-byte loads of four profile words, stored word-major
-        for (int idx = tid; idx < kET * (kW / 4); idx += 256) {
-            const int r = idx / (kW / 4), q = idx % (kW / 4);
-            const uint4 va = reinterpret_cast<const uint4*>(prof)[(i0 + r) * (kW / 4) + q];
-            const uint4 vb = reinterpret_cast<const uint4*>(prof)[(j0 + r) * (kW / 4) + q];
-            pa[4 * q + 0][r] = va.x;
-            pa[4 * q + 1][r] = va.y;
-            pa[4 * q + 2][r] = va.z;
-            pa[4 * q + 3][r] = va.w;
-            pb[4 * q + 0][r] = vb.x;
-            pb[4 * q + 1][r] = vb.y;
-            pb[4 * q + 2][r] = vb.z;
-            pb[4 * q + 3][r] = vb.w;
-        }
-        for (int r = tid; r < kET; r += 256) {
-            la[r] = i0 + r < n ? slen[i0 + r] : 0xffffffffu;
-            lb[r] = j0 + r < n ? slen[j0 + r] : 0xffffffffu;
-        }
-        __syncthreads();
-        uint32_t l1s[8][8];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp; p < n_pad; p += nwarps) {
+        // lane l: bins 2 l and 2 l + 1 (bytes 2 (l % 2) .. of profile word l / 2)
+        const uint32_t wv = prof[p * (kBins / 4) + (lane >> 1)];
+        const uint32_t c0 = (wv >> (16 * (lane & 1))) & 0xffu, c1 = (wv >> (16 * (lane & 1) + 8)) & 0xffu;
+        uint32_t q[4];
 #pragma unroll
-        for (int r = 0; r < 8; ++r)
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t cnt = w < 2 ? c0 : c1;
+            uint32_t v = 0;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) l1s[r][c] = 0;
-#pragma unroll 2
-        for (int k = 0; k < kW; ++k) {
-            const uint4 a0 = *reinterpret_cast<const uint4*>(&pa[k][ty * 8]);
-            const uint4 a1 = *reinterpret_cast<const uint4*>(&pa[k][ty * 8 + 4]);
-            const uint4 b0 = *reinterpret_cast<const uint4*>(&pb[k][tx * 8]);
-            const uint4 b1 = *reinterpret_cast<const uint4*>(&pb[k][tx * 8 + 4]);
-            const uint32_t av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const uint32_t bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-#pragma unroll
-                for (int c = 0; c < 8; ++c) l1s[r][c] = __vsadu4(av[r], bv[c]) + l1s[r][c];
+            for (int b = 0; b < 4; ++b) v |= (cnt > (uint32_t)(4 * (w & 1) + b) ? 0x38u : 0u) << (8 * b);
+            q[w] = v;
         }
-        uint64_t mask = 0;  // 8 x 8 block of this thread
+        reinterpret_cast<uint4*>(x8 + p * kFilterBytes)[lane] = make_uint4(q[0], q[1], q[2], q[3]);
+        float nn = (float)(min(c0, 8u) + min(c1, 8u));
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int ra = ty * 8 + r;
-            const uint32_t l1 = la[ra];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                const int cb = tx * 8 + c;
-                const uint32_t l2 = lb[cb];
-                const uint32_t dl = l1 > l2 ? l1 - l2 : l2 - l1;
-                const bool ok = (l1 != 0xffffffffu) && (l2 != 0xffffffffu) && dl <= (uint32_t)K &&
-                                (tp.x != tp.y || ra < cb) && l1s[r][c] <= thr;
-                mask |= (uint64_t)(ok ? 1u : 0u) << (r * 8 + c);
-            }
+        for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+        if (lane == 0) {
+            rowinfo[p] = make_float4(nn, 0.f, 0.f, nn);
+            ucol[p] = nn;
         }
-        const int nhit = __popcll(mask);
-        int incl = nhit;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        if (lane == 31) s_warp[warp] = incl;
-        __syncthreads();
-        if (tid == 0) {
-            int a = 0;
-            for (int k = 0; k < 8; ++k) { const int t = s_warp[k]; s_warp[k] = a; a += t; }
-            s_base = a ? atomicAdd(ccount, (unsigned long long)a) : 0ull;
-        }
-        __syncthreads();
-        unsigned long long pos = s_base + (unsigned long long)(s_warp[warp] + incl - nhit);
-        while (mask) {
-            const int b = __ffsll((long long)mask) - 1;
-            mask &= mask - 1;
-            if (pos < cap) cand[pos] = make_uint2((uint32_t)(i0 + ty * 8 + b / 8), (uint32_t)(j0 + tx * 8 + b % 8));
-            ++pos;
-        }
+    }
+}
+
+// Per tile: {0, largest n of its rows} (the kernel's column-tile term; no error radii).
+__global__ void k_edit_tileinfo(const float4* __restrict__ rowinfo, int64_t T, float2* __restrict__ tileinfo)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+        float m = 0.f;
+        for (int r = 0; r < kET; ++r) m = fmaxf(m, rowinfo[t * kET + r].x);
+        tileinfo[t] = make_float2(0.f, m);
     }
 }
 
@@ -277,7 +225,8 @@ __global__ void __launch_bounds__(256) k_edit_verify(const uint8_t* __restrict__
             const int64_t oa = off[perm[c.x]], ob = off[perm[c.y]];
             const int ma = (int)(off[perm[c.x] + 1] - oa), mb = (int)(off[perm[c.y] + 1] - ob);
             // the reference computes EditDistance(indexed point, query); the distance is symmetric
-            dist = banded_edit<B>(atoms + oa, ma, atoms + ob, mb, K);
+            // and at least the length difference
+            dist = (ma > mb ? ma - mb : mb - ma) > K ? K + 1 : banded_edit<B>(atoms + oa, ma, atoms + ob, mb, K);
             hit = dist <= K;
         }
         const unsigned ball = __ballot_sync(0xffffffffu, hit);
@@ -368,7 +317,9 @@ __global__ void __launch_bounds__(256) k_edit_verify_bp(const uint8_t* __restric
             const uint8_t* pat = atoms + (a_pat ? oa : ob);
             const uint8_t* txt = atoms + (a_pat ? ob : oa);
             const int m = a_pat ? ma : mb, n = a_pat ? mb : ma;
-            if (m == 0) {
+            if (n - m > K) {
+                dist = K + 1;  // the distance is at least the length difference
+            } else if (m == 0) {
                 dist = n;
             } else {
 #pragma unroll
@@ -635,28 +586,42 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             c->stats.tile_pairs = npairs;
             c->stats.tile_pairs_all = T * (T + 1) / 2;
             c->stats.pairs_evaluated = (int64_t)npairs * kET * kET;
-            // 3. filter
+            // 3. filter on the tensor cores: the capped-profile L1 of every string pair of the
+            //    tile pairs as a Gram form over thermometer-coded 8-bit rows (k_edit_thermo)
             c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
             unsigned long long* ccount = c->counters.as<unsigned long long>() + 2;
             unsigned long long* ecount = c->counters.as<unsigned long long>() + 3;
-            unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
             unsigned long long got = 0;
-            const unsigned gf = (unsigned)std::max<int64_t>(1, std::min<int64_t>(npairs, (int64_t)c->num_sms * 8));
-            for (int attempt = 0;; ++attempt) {
-                c->cand.reserve(sizeof(uint2) * ccap);
+            if (npairs > 0) {
+                c->xb_sorted.reserve((size_t)n_pad * kFilterBytes);
+                c->norms.reserve(sizeof(float4) * (size_t)n_pad + sizeof(float) * (size_t)n_pad +
+                                 sizeof(float2) * (size_t)T + 64);
+                uint8_t* x8 = c->xb_sorted.as<uint8_t>();
+                float4* rowinfo = c->norms.as<float4>();
+                float* ucol = (float*)(rowinfo + n_pad);
+                float2* tileinfo = (float2*)(((uintptr_t)(ucol + n_pad) + 15) & ~(uintptr_t)15);
+                k_edit_thermo<<<(unsigned)std::min<int64_t>(ceil_div(n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0,
+                                s>>>(prof, n_pad, x8, rowinfo, ucol);
+                k_edit_tileinfo<<<gt, 256, 0, s>>>(rowinfo, T, tileinfo);
+                c->launches += 2;
+                Layout Le;
+                Le.n = n;
+                Le.n_pad = n_pad;
+                Le.T = T;
+                Le.d = kFilterBytes;
+                Le.pairs = c->pair_list.as<int2>();
+                Le.tile_pairs = (unsigned long long)npairs;
+                schedule_items(c, Le, c->num_sms, 1);
+                // thr^2 (as the kernel squares it in FP32) in [2 q K, 2 q K + 1): the integer test
+                // L1 <= 2 q K exactly
+                const float lim = (float)(2 * kQ * K);
+                float thr = std::sqrt(lim);
+                while (thr * thr < lim) thr = std::nextafter(thr, INFINITY);
+                got = run_filter_f8(c, Le, x8, rowinfo, ucol, tileinfo, thr, ccount);
+            } else {
                 RNNG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), s));
-                if (npairs > 0) {
-                    k_edit_filter<<<gf, 256, 0, s>>>(prof, slen, n, c->pair_list.as<int2>(), npairs, K,
-                                                     c->cand.as<uint2>(), ccount, ccap);
-                    ++c->launches;
-                }
-                RNNG_CUDA(cudaMemcpyAsync(&got, ccount, sizeof(got), cudaMemcpyDeviceToHost, s));
-                RNNG_CUDA(cudaStreamSynchronize(s));
-                if (got <= ccap) break;
-                RNNG_REQUIRE(attempt < 2, RNNG_ERR_OVERFLOW, "candidate buffer overflow after regrowth");
-                ccap = got + got / 8 + 1024;
             }
-            c->cand_cap_hint = std::max<unsigned long long>(c->cand_cap_hint, got + got / 8);
+            const unsigned long long ccap = std::max<unsigned long long>(got, 1ull);
             c->stats.candidates = (int64_t)got;
             // 4. exact verification: Myers' bit-vector algorithm when the alphabet has at most
             //    kBpMaxSym symbols and no string is longer than kBpMaxLen, else the banded DP

@@ -75,4 +75,13 @@ bool bf16_supported(int d);
 // Column tiles per Gram item for dimension d (2: N = 256 MMAs, 1: N = 128).
 int gram_item_tiles(int d);
 
+// Filter rows of 0/1 values as E4M3 bytes (0x00 / 0x38), kFilterBytes per row, n_pad rows in
+// the tile order of L: candidate pairs (i < j) of L's scheduled items whose
+// n_i + n_j - 2 x_i.x_j <= thr_sqrt^2 (rowinfo[i] = {n_i, 0, 0, n_i}, ucol = n, tileinfo
+// = {0, max n of the tile}; integer-exact) by the tensor-core kernel on 8-bit operands.
+// Candidates in c->cand, their count in *cnt (returned).
+constexpr int kFilterBytes = 512;
+unsigned long long run_filter_f8(rnng_ctx* c, const Layout& L, const uint8_t* x8, const float4* rowinfo,
+                                 const float* ucol, const float2* tileinfo, float thr_sqrt, unsigned long long* cnt);
+
 }  // namespace rnng

@@ -195,6 +195,17 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint6
         : "memory");
 }
 
+// The same MMA on 8-bit operands (kind::f8f6f4; the 0/1 filter operands, E4M3 both).
+__device__ __forceinline__ void umma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate)
+{
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t* bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -258,6 +269,13 @@ __host__ __device__ constexpr uint32_t gram_idesc(int nt)
            ((uint32_t)(kTile >> 4) << 24);
 }
 
+// Instruction descriptor for kind::f8f6f4: D f32, A and B E4M3 (format 0), both K-major,
+// M = 128, N = 128 nt.
+__host__ __device__ constexpr uint32_t gram_idesc_f8(int nt)
+{
+    return (1u << 4) | ((uint32_t)((kAccCols * nt) >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+}
+
 // Four-deep register prefetch of the item list, so that the dependent global load of
 // the next item is issued several items ahead of its use.
 struct ItemPrefetch {
@@ -305,7 +323,8 @@ struct ItemPrefetch {
 // KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item; FOLD: the column
 // tiles come from tmapB with the column terms folded into their padding (k_to_bf16), so
 // the accumulator already holds g - u_j / 2 and the test needs no u_j
-template <int KCH, int NT, bool FOLD>
+// F8: 8-bit operands (E4M3; 128 per 128-byte chunk row, K = 32 per MMA), same byte layout.
+template <int KCH, int NT, bool FOLD, bool F8>
 __global__ void __maxnreg__(kGramMaxRegs)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmapB,
                 const int4* __restrict__ items, unsigned long long nitems,
@@ -315,7 +334,8 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 const unsigned long long* __restrict__ sched, int* __restrict__ fault)
 {
     constexpr int kAcc = kTmemCols / (kAccCols * NT);  // accumulators in flight
-    constexpr uint32_t kIdesc = gram_idesc(NT);
+    constexpr uint32_t kIdesc = F8 ? gram_idesc_f8(NT) : gram_idesc(NT);
+    constexpr int kChunkElems = F8 ? 2 * kChunkK : kChunkK;  // elements per 128-byte chunk row
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
     const GramSmem SL = GramSmem::make(KCH, NT);
@@ -383,7 +403,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     mbar_expect_tx(a_full, kTileBytes);
 #pragma unroll
                     for (int kc = 0; kc < KCH; ++kc)
-                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkK, it.x * kTile);
+                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkElems, it.x * kTile);
                     ++aloads;
                     cur_i = it.x;
                 }
@@ -395,9 +415,10 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 // stacked rows of one 128 NT-row operand
 #pragma unroll
                 for (int kc = 0; kc < KCH; ++kc) {
-                    tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkK, it.y * kTile);
+                    tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems, it.y * kTile);
                     if (second)
-                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkK, it.z * kTile);
+                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems,
+                                    it.z * kTile);
                 }
                 issued |= 1u << q;
                 last_phase = (last_phase & ~(1u << q)) | (ph << q);
@@ -452,9 +473,14 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 for (int kc = 0; kc < KCH; ++kc)
 #pragma unroll
                     for (int k = 0; k < kChunkK / 16; ++k)
-                        umma_bf16(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
-                                  bdesc_q + (uint64_t)(kc * NT * (kChunkBytes >> 4) + 2 * k), kIdesc,
-                                  (kc | k) != 0 ? 1u : 0u);
+                        if constexpr (F8)
+                            umma_f8(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
+                                      bdesc_q + (uint64_t)(kc * NT * (kChunkBytes >> 4) + 2 * k), kIdesc,
+                                      (kc | k) != 0 ? 1u : 0u);
+                        else
+                            umma_bf16(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
+                                      bdesc_q + (uint64_t)(kc * NT * (kChunkBytes >> 4) + 2 * k), kIdesc,
+                                      (kc | k) != 0 ? 1u : 0u);
                 any = true;
                 umma_commit(&b_empty[q]);
                 umma_commit(&tfull[b]);
@@ -1099,7 +1125,7 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int KCH, int NT, bool FOLD>
+template <int KCH, int NT, bool FOLD, bool F8>
 static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, const CUtensorMap& tm,
                           const CUtensorMap& tmb, const int4* items,
                           unsigned long long nitems, const float4* rowinfo, const float* ucol, const float2* tileinfo,
@@ -1107,11 +1133,11 @@ static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, co
                           unsigned long long ccap, const unsigned long long* sched, int* fault)
 {
     if (!launch) {
-        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem));
         return;
     }
-    k_gram_bf16<KCH, NT, FOLD><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
+    k_gram_bf16<KCH, NT, FOLD, F8><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
                                                                 eps_p, kappa, cand, cnt, ccap, sched, fault);
 }
 
@@ -1120,22 +1146,23 @@ template <bool FOLD, class... Args>
 static void gram_dispatch_fold(int kch, int nt, Args... args)
 {
     if (nt == 2) {
-        if (kch == 1) gram_instance<1, 2, FOLD>(args...);
-        else gram_instance<2, 2, FOLD>(args...);
+        if (kch == 1) gram_instance<1, 2, FOLD, false>(args...);
+        else gram_instance<2, 2, FOLD, false>(args...);
     } else {
         switch (kch) {
-            case 1: gram_instance<1, 1, FOLD>(args...); break;
-            case 2: gram_instance<2, 1, FOLD>(args...); break;
-            case 3: gram_instance<3, 1, FOLD>(args...); break;
-            default: gram_instance<4, 1, FOLD>(args...); break;
+            case 1: gram_instance<1, 1, FOLD, false>(args...); break;
+            case 2: gram_instance<2, 1, FOLD, false>(args...); break;
+            case 3: gram_instance<3, 1, FOLD, false>(args...); break;
+            default: gram_instance<4, 1, FOLD, false>(args...); break;
         }
     }
 }
 
 template <class... Args>
-static void gram_dispatch(bool fold, int kch, int nt, Args... args)
+static void gram_dispatch(bool fold, bool f8, int kch, int nt, Args... args)
 {
-    if (fold) gram_dispatch_fold<true>(kch, nt, args...);
+    if (f8) gram_instance<4, 1, false, true>(args...);  // the 0/1 filter operand: 512 bytes per row
+    else if (fold) gram_dispatch_fold<true>(kch, nt, args...);
     else gram_dispatch_fold<false>(kch, nt, args...);
 }
 
@@ -1145,37 +1172,34 @@ int gram_item_tiles(int d)
     return ceil_div(d, kChunkK) <= 2 ? 2 : 1;
 }
 
-void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
+// Candidates of the scheduled items of L by the tensor-core kernel, with the candidate
+// buffer regrown (at most twice) until it holds them all; the count is left in *cnt and
+// returned.
+static unsigned long long gram_candidates(rnng_ctx* c, const Layout& L, const CUtensorMap& tm,
+                                          const CUtensorMap& tmb, int kchunks, int nt, bool fold, bool f8,
+                                          const float4* rowinfo, const float* ucol, const float2* tileinfo,
+                                          float eps_p, unsigned long long* cnt)
 {
     cudaStream_t s = c->stream;
-    const int kchunks = c->bf16_dp / kChunkK;
-    const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(c->tmap);
-    unsigned long long* cnt = c->counters.as<unsigned long long>() + 5;
     unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
-    const int nt = L.item_tiles;
     const GramSmem layout = GramSmem::make(kchunks, nt);
     RNNG_REQUIRE(layout.nslots >= 2, RNNG_ERR_UNSUPPORTED, "BF16 operand tiles too large for shared memory");
     const size_t smem = layout.total + 1024;
-    const float4* rowinfo = (const float4*)c->bf16_rowinfo;
-    const float* ucol = (const float*)c->bf16_ucol;
-    const float2* tileinfo = (const float2*)c->bf16_tileinfo;
-    const CUtensorMap& tmb = *reinterpret_cast<const CUtensorMap*>(c->tmapB);
-    const bool fold = c->bf16_fold;
-    gram_dispatch(fold, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n,
-                  c->bf16_eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
+    gram_dispatch(fold, f8, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
+                  L.n, eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
     const int grid = L.sched_G;
     RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
     const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
+    unsigned long long got = 0;
     for (int attempt = 0;; ++attempt) {
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
-        gram_dispatch(fold, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
-                      L.n, c->bf16_eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+        gram_dispatch(fold, f8, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol,
+                      tileinfo, L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
         ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));
-        unsigned long long got = 0;
         RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
         {
@@ -1185,7 +1209,6 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         int fw = 0;
         RNNG_CUDA(cudaMemcpy(&fw, c->fault_word, sizeof(int), cudaMemcpyDeviceToHost));
         RNNG_REQUIRE(fw == FAULT_NONE, RNNG_ERR_DEVICE, "Gram kernel: bounded wait ran out (fault word set)");
-        c->last_candidates = (int64_t)got;
         if (got <= ccap) {
             c->cand_cap_hint = std::max<unsigned long long>(c->cand_cap_hint, got + got / 8);
             break;
@@ -1194,6 +1217,36 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         ccap = got + got / 8 + 1024;
         c->stats.retries++;
     }
+    return got;
+}
+
+unsigned long long run_filter_f8(rnng_ctx* c, const Layout& L, const uint8_t* x8, const float4* rowinfo,
+                                 const float* ucol, const float2* tileinfo, float thr_sqrt, unsigned long long* cnt)
+{
+    CUtensorMap& tm = *reinterpret_cast<CUtensorMap*>(c->tmap);
+    cuuint64_t gdim[2] = {(cuuint64_t)kFilterBytes, (cuuint64_t)L.n_pad};
+    cuuint64_t gstride[1] = {(cuuint64_t)kFilterBytes};
+    cuuint32_t box[2] = {(cuuint32_t)(2 * kChunkK), (cuuint32_t)kTile};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = get_encode()(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)x8, gdim, gstride, box, estride,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return gram_candidates(c, L, tm, tm, kFilterBytes / (2 * kChunkK), 1, false, true, rowinfo, ucol, tileinfo,
+                           thr_sqrt, cnt);
+}
+
+void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
+{
+    cudaStream_t s = c->stream;
+    const int kchunks = c->bf16_dp / kChunkK;
+    const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(c->tmap);
+    const CUtensorMap& tmb = *reinterpret_cast<const CUtensorMap*>(c->tmapB);
+    unsigned long long* cnt = c->counters.as<unsigned long long>() + 5;
+    c->last_candidates = (int64_t)gram_candidates(
+        c, L, tm, tmb, kchunks, L.item_tiles, c->bf16_fold, false, (const float4*)c->bf16_rowinfo,
+        (const float*)c->bf16_ucol, (const float2*)c->bf16_tileinfo, c->bf16_eps_p, cnt);
+    const unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
     RNNG_CUDA(cudaEventRecord(c->ev[8], s));
     const unsigned long long ncand = (unsigned long long)c->last_candidates;
     const int rthreads = 32 * kRecheckWarps;

@@ -136,6 +136,59 @@ __global__ void k_edit_thermo(const uint32_t* __restrict__ prof, int64_t n_pad, 
     }
 }
 
+// Filter operand for alphabets of at most 4 symbols (symmap codes 0..3): exact 4-grams,
+// bin = the 4-gram's base-4 code (256 bins, no collisions), counts capped at 2, bin b's
+// two levels at bytes 2 b and 2 b + 1.  Then n_a + n_b - 2 x_a.x_b is the L1 distance of
+// the capped 4-gram profiles, <= 2 q K = 8 K for strings within K.  One warp per row,
+// its counts in shared memory; rows in length-sorted order.
+__global__ void __launch_bounds__(256) k_edit_thermo_q4(const uint8_t* __restrict__ atoms,
+                                                        const int64_t* __restrict__ off,
+                                                        const int32_t* __restrict__ perm, int64_t n, int64_t n_pad,
+                                                        const uint8_t* __restrict__ symmap, uint8_t* __restrict__ x8,
+                                                        float4* __restrict__ rowinfo, float* __restrict__ ucol)
+{
+    __shared__ uint32_t cnt[8][256];
+    __shared__ uint8_t smap[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) smap[k] = symmap[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
+    uint32_t* h = cnt[wb];
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t p = warp; p < n_pad; p += nwarps) {
+        for (int b = lane; b < 256; b += 32) h[b] = 0;
+        __syncwarp();
+        if (p < n) {
+            const int64_t o = off[perm[p]], m = off[perm[p] + 1] - o;
+            for (int64_t i = lane; i + 4 <= m; i += 32) {
+                const uint32_t code = ((uint32_t)smap[atoms[o + i]] << 6) | ((uint32_t)smap[atoms[o + i + 1]] << 4) |
+                                      ((uint32_t)smap[atoms[o + i + 2]] << 2) | (uint32_t)smap[atoms[o + i + 3]];
+                atomicAdd(&h[code], 1u);
+            }
+        }
+        __syncwarp();
+        // lane l: bins 8 l .. 8 l + 7 -> bytes 16 l .. 16 l + 15
+        uint32_t q[4];
+        uint32_t nn = 0;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t c0 = h[8 * lane + 2 * w], c1 = h[8 * lane + 2 * w + 1];
+            q[w] = (c0 > 0 ? 0x38u : 0u) | (c0 > 1 ? 0x38u : 0u) << 8 | (c1 > 0 ? 0x38u : 0u) << 16 |
+                   (c1 > 1 ? 0x38u : 0u) << 24;
+            nn += min(c0, 2u) + min(c1, 2u);
+        }
+        reinterpret_cast<uint4*>(x8 + p * kFilterBytes)[lane] = make_uint4(q[0], q[1], q[2], q[3]);
+        float nf = (float)nn;
+#pragma unroll
+        for (int o2 = 16; o2 > 0; o2 >>= 1) nf += __shfl_xor_sync(0xffffffffu, nf, o2);
+        if (lane == 0) {
+            rowinfo[p] = make_float4(nf, 0.f, 0.f, nf);
+            ucol[p] = nf;
+        }
+        __syncwarp();
+    }
+}
+
 // Per tile: {0, largest n of its rows} (the kernel's column-tile term; no error radii).
 __global__ void k_edit_tileinfo(const float4* __restrict__ rowinfo, int64_t T, float2* __restrict__ tileinfo)
 {
@@ -560,12 +613,42 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             c->cub_tmp.reserve(tmp);
             RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, len, slen, idx, perm, (int)n, 0, 32, s));
             c->launches += cub_sort_kernels(n, 32);
-            // 2. profiles and tile length ranges
+            // 2. the alphabet (byte histogram; its symbols numbered in byte order), then the
+            //    filter profiles and tile length ranges: exact 4-grams over at most 4 symbols,
+            //    else hashed 3-grams
+            uint32_t maxlen = 0;
+            int64_t total_atoms = 0;
+            RNNG_CUDA(cudaMemcpyAsync(&maxlen, slen + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            RNNG_CUDA(cudaMemcpyAsync(&total_atoms, doff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+            c->sym.reserve(256 * sizeof(unsigned int) + 256);
+            unsigned int* hist = c->sym.as<unsigned int>();
+            uint8_t* symmap = (uint8_t*)(hist + 256);
+            RNNG_CUDA(cudaMemsetAsync(hist, 0, 256 * sizeof(unsigned int), s));
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            if (total_atoms > 0) {  // offsets start at 0 (RNNG's layout)
+                k_byte_hist<<<(unsigned)std::min<int64_t>(ceil_div(total_atoms, 256), (int64_t)c->num_sms * 4), 256, 0,
+                              s>>>(datoms, total_atoms, hist);
+                ++c->launches;
+            }
+            unsigned int h[256];
+            RNNG_CUDA(cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, s));
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            uint8_t map[256];
+            int nsym = 0;
+            for (int b = 0; b < 256; ++b) map[b] = h[b] ? (uint8_t)(nsym++) : (uint8_t)0;
+            if (nsym <= kBpMaxSym) {
+                RNNG_CUDA(cudaMemcpyAsync(symmap, map, 256, cudaMemcpyHostToDevice, s));
+                RNNG_CUDA(cudaStreamSynchronize(s));  // map lifetime
+            }
+            const bool exact4 = nsym <= 4;
+            const int qf = exact4 ? 4 : kQ;  // q of the filter's q-grams
             c->x_sorted.reserve(sizeof(uint32_t) * (size_t)n_pad * (kBins / 4));
             uint32_t* prof = c->x_sorted.as<uint32_t>();
-            k_edit_profiles<<<(unsigned)std::min<int64_t>(T, (int64_t)c->num_sms * 8), 128, 0, s>>>(
-                datoms, doff, perm, n, n_pad, prof);
-            ++c->launches;
+            if (!exact4) {
+                k_edit_profiles<<<(unsigned)std::min<int64_t>(T, (int64_t)c->num_sms * 8), 128, 0, s>>>(
+                    datoms, doff, perm, n, n_pad, prof);
+                ++c->launches;
+            }
             c->aux2.reserve(sizeof(uint32_t) * 2 * (size_t)T + sizeof(int32_t) * 2 * ((size_t)T + 1));
             uint32_t* tlo = c->aux2.as<uint32_t>();
             uint32_t* thi = tlo + T;
@@ -587,7 +670,8 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             c->stats.tile_pairs_all = T * (T + 1) / 2;
             c->stats.pairs_evaluated = (int64_t)npairs * kET * kET;
             // 3. filter on the tensor cores: the capped-profile L1 of every string pair of the
-            //    tile pairs as a Gram form over thermometer-coded 8-bit rows (k_edit_thermo)
+            //    tile pairs as a Gram form over thermometer-coded 8-bit rows (k_edit_thermo_q4,
+            //    k_edit_thermo)
             c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
             unsigned long long* ccount = c->counters.as<unsigned long long>() + 2;
             unsigned long long* ecount = c->counters.as<unsigned long long>() + 3;
@@ -600,8 +684,11 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
                 float4* rowinfo = c->norms.as<float4>();
                 float* ucol = (float*)(rowinfo + n_pad);
                 float2* tileinfo = (float2*)(((uintptr_t)(ucol + n_pad) + 15) & ~(uintptr_t)15);
-                k_edit_thermo<<<(unsigned)std::min<int64_t>(ceil_div(n_pad * 32, 256), (int64_t)c->num_sms * 16), 256, 0,
-                                s>>>(prof, n_pad, x8, rowinfo, ucol);
+                const unsigned gth = (unsigned)std::min<int64_t>(ceil_div(n_pad * 32, 256), (int64_t)c->num_sms * 16);
+                if (exact4)
+                    k_edit_thermo_q4<<<gth, 256, 0, s>>>(datoms, doff, perm, n, n_pad, symmap, x8, rowinfo, ucol);
+                else
+                    k_edit_thermo<<<gth, 256, 0, s>>>(prof, n_pad, x8, rowinfo, ucol);
                 k_edit_tileinfo<<<gt, 256, 0, s>>>(rowinfo, T, tileinfo);
                 c->launches += 2;
                 Layout Le;
@@ -614,7 +701,7 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
                 schedule_items(c, Le, c->num_sms, 1);
                 // thr^2 (as the kernel squares it in FP32) in [2 q K, 2 q K + 1): the integer test
                 // L1 <= 2 q K exactly
-                const float lim = (float)(2 * kQ * K);
+                const float lim = (float)(2 * qf * K);
                 float thr = std::sqrt(lim);
                 while (thr * thr < lim) thr = std::nextafter(thr, INFINITY);
                 got = run_filter_f8(c, Le, x8, rowinfo, ucol, tileinfo, thr, ccount);
@@ -625,37 +712,7 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
             c->stats.candidates = (int64_t)got;
             // 4. exact verification: Myers' bit-vector algorithm when the alphabet has at most
             //    kBpMaxSym symbols and no string is longer than kBpMaxLen, else the banded DP
-            bool use_bp = false;
-            if (got > 0) {
-                uint32_t maxlen = 0;
-                int64_t total_atoms = 0;
-                RNNG_CUDA(cudaMemcpyAsync(&maxlen, slen + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-                RNNG_CUDA(cudaMemcpyAsync(&total_atoms, doff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-                RNNG_CUDA(cudaStreamSynchronize(s));
-                if (maxlen <= (uint32_t)kBpMaxLen) {
-                    c->sym.reserve(256 * sizeof(unsigned int) + 256);
-                    unsigned int* hist = c->sym.as<unsigned int>();
-                    uint8_t* symmap = (uint8_t*)(hist + 256);
-                    RNNG_CUDA(cudaMemsetAsync(hist, 0, 256 * sizeof(unsigned int), s));
-                    const int64_t natoms_all = total_atoms;  // offsets start at 0 (RNNG's layout)
-                    if (natoms_all > 0) {
-                        k_byte_hist<<<(unsigned)std::min<int64_t>(ceil_div(natoms_all, 256), (int64_t)c->num_sms * 4),
-                                      256, 0, s>>>(datoms, natoms_all, hist);
-                        ++c->launches;
-                    }
-                    unsigned int h[256];
-                    RNNG_CUDA(cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, s));
-                    RNNG_CUDA(cudaStreamSynchronize(s));
-                    uint8_t map[256];
-                    int nsym = 0;
-                    for (int b = 0; b < 256; ++b) map[b] = h[b] ? (uint8_t)(nsym++) : (uint8_t)0;
-                    if (nsym <= kBpMaxSym) {
-                        RNNG_CUDA(cudaMemcpyAsync(symmap, map, 256, cudaMemcpyHostToDevice, s));
-                        RNNG_CUDA(cudaStreamSynchronize(s));  // map lifetime
-                        use_bp = true;
-                    }
-                }
-            }
+            const bool use_bp = got > 0 && maxlen <= (uint32_t)kBpMaxLen && nsym <= kBpMaxSym;
             unsigned long long ecap = std::max<unsigned long long>(1u << 20, c->edge_cap_hint);
             unsigned long long egot = 0;
             const unsigned gv = (unsigned)std::max<unsigned long long>(

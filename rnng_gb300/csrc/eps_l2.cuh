@@ -50,8 +50,9 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E);
 void finalize_edges(rnng_ctx* c, const Layout& L, const int64_t* d_ids, const EdgeOut& E, int64_t m, int64_t* u,
                     int64_t* v, float* w);
+// Stable sort of (key, value) pairs by key bits [begin_bit, end_bit).
 void sort_pairs_u64(rnng_ctx* c, uint64_t* keys_in, uint64_t* keys_out, int32_t* vals_in, int32_t* vals_out,
-                    int64_t n, int end_bit);
+                    int64_t n, int end_bit, int begin_bit = 0);
 // out[0..count-1] = exclusive prefix sum of in[0..count-2] (in[count-1] is zeroed first).
 void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t count);
 

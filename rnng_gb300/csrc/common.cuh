@@ -34,13 +34,13 @@ struct Error {
         if (!(cond)) throw ::rnng::Error{(code), (text)}; \
     } while (0)
 
-// A growable device buffer owned by the context.  Buffers are reused across calls
-// so that steady-state calls do not allocate.
 // Slots of the context's 64-bit device counter array (counters): 0-1 pruning, 2-3 edit counts,
 // 4 edges, 5 candidates, 6 query hits, 9 edit maximum length, 10-11 rips checks,
 // 12 ball widening (two floats).
 constexpr int kCounterSlots = 16;
 
+// A growable device buffer owned by the context.  Buffers are reused across calls
+// so that steady-state calls do not allocate.
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;

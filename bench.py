@@ -420,6 +420,20 @@ def run_secondary(args, world, rank, local):
         assert u == units
     e2e_s = statistics.median(t_e2e)
     roofline = None
+    if wl == "k3" and last["ms_gram"] > 0:
+        # the filter: a Gram form over 512-byte E4M3 rows (thermometer-coded q-gram profiles)
+        peak = 2 * 1900.0
+        src = "2 x fallback bf16 (FP8 dense rate is twice BF16's)"
+        try:
+            peak = 2.0 * float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops_sustained"])
+            src = "2 x measured sustained bf16 (FP8 dense rate is twice BF16's)"
+        except (OSError, KeyError, ValueError):
+            pass
+        flops = 2.0 * 512 * last["pairs_evaluated"]
+        achieved = flops / (statistics.median(s["ms_gram"] for s in stats) / 1e3) / 1e12
+        roofline = {"bound": "tensor", "kernel": "k_gram_bf16 (FP8 filter)", "achieved": achieved, "peak": peak,
+                    "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": src, "traffic": None,
+                    "algorithmic": "2*512 ops per evaluated string pair (512 E4M3 profile bytes per string)"}
     if wl in ("k1", "k5") and last["ms_gram"] > 0:
         peak = 1900.0
         src = "of fallback"

@@ -92,7 +92,7 @@ typedef struct rnng_stats {
     int64_t retries;        /* edge-buffer regrowths */
     int64_t simplices;      /* Rips: simplices emitted */
     int64_t kernel_launches;/* kernels launched by the call */
-    double ms_gram;         /* BF16 mode: device time of the tensor-core Gram kernel */
+    double ms_gram;         /* device time of the tensor-core Gram kernel (BF16 mode; the edit filter) */
     double prune_widen;     /* mean relative widening of the tensor-core ball test (d <= 256) */
     int64_t prune_tensor;   /* 1: tile pairs pruned by the tensor-core ball test, 0: by the FP32 one */
 } rnng_stats;

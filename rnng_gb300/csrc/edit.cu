@@ -569,6 +569,7 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
         RNNG_REQUIRE(radius == radius, RNNG_ERR_INVALID, "radius is NaN");
         c->stats = rnng_stats{};
         c->launches = 0;
+        c->gram_ms = 0.0;
         cudaStream_t s = c->stream;
         const int K = radius < 0.f ? -1 : (int)std::min(std::floor((double)radius), 1e9);
         RNNG_REQUIRE(K <= 32, RNNG_ERR_UNSUPPORTED, "edit-distance radius above 32 is not supported");
@@ -770,6 +771,7 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
         RNNG_CUDA(cudaStreamSynchronize(s));
         c->stats.edges = m;
         c->stats.kernel_launches = c->launches;
+        c->stats.ms_gram = c->gram_ms;  // the tensor-core filter
     });
 }
 

@@ -565,16 +565,6 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
 // for both operands (a dot product does not depend on it) so that every lane fetches
 // its fragments with 16-byte loads: lane (g, t) reads columns 8t .. 8t + 7, which feed
 // k-slots {2t, 2t+1, 2t+8, 2t+9} of two consecutive k-steps.
-__device__ __forceinline__ void mma_bf16_16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                               uint32_t b0, uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
 constexpr int kSB = kSuper * kBalls;  // balls per super-tile (32)
 
 __global__ void __launch_bounds__(256) k_tile_close_mma(const int2* __restrict__ supers,

@@ -159,4 +159,18 @@ __device__ __forceinline__ float l2seq_acc(float acc, float a, float b)
     return __fadd_rn(acc, __fmul_rn(d, d));
 }
 
+// Warp-level tensor-core product c += A B (mma.sync m16n8k16, BF16 operands, FP32
+// accumulator) on the standard fragments: a0..a3 = A rows (g, g + 8) x k-slots
+// (2t, 2t + 1) and (2t + 8, 2t + 9); b0, b1 = B column g x the same k-slots; c0..c3 =
+// rows (g, g + 8) x columns (2t, 2t + 1), with g = lane / 4, t = lane % 4.
+__device__ __forceinline__ void mma_bf16_16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 }  // namespace rnng

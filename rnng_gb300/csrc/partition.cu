@@ -106,15 +106,6 @@ __global__ void __launch_bounds__(256) k_assign(const float* __restrict__ X, con
 // stream through in chunks of 32.  Inside each 32-dimension group the k order is
 // permuted the same way for both operands: lane (g, t) holds dimensions 8t .. 8t + 7,
 // which feed k-slots {2t, 2t+1, 2t+8, 2t+9} of two consecutive k-steps.
-__device__ __forceinline__ void mma_16816(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                          uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
 
 // Eight dimensions 32 kp + 8 t .. + 7 of row `src` of X (zero outside d), shifted and
 // rounded to four BF16 pairs; adds their squares to nrm.
@@ -221,8 +212,8 @@ __global__ void __launch_bounds__(256) k_assign_mma(const float* __restrict__ X,
             }
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
-                mma_16816(acc[nt], af[kp][0][0], af[kp][1][0], af[kp][0][1], af[kp][1][1], bf[nt].x, bf[nt].y);
-                mma_16816(acc[nt], af[kp][0][2], af[kp][1][2], af[kp][0][3], af[kp][1][3], bf[nt].z, bf[nt].w);
+                mma_bf16_16816(acc[nt], af[kp][0][0], af[kp][1][0], af[kp][0][1], af[kp][1][1], bf[nt].x, bf[nt].y);
+                mma_bf16_16816(acc[nt], af[kp][0][2], af[kp][1][2], af[kp][0][3], af[kp][1][3], bf[nt].z, bf[nt].w);
             }
         }
         // acc[nt][2 h + e] = row g + 8 h, column c0 + 8 nt + 2 t + e

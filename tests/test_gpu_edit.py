@@ -70,3 +70,33 @@ def test_k3_full_size_rows_sample(ctx, orc):
         wu, wv, ww = orc.eps_graph_edit(atoms, offsets, r, rows=(r0, r1))
         sel = (u >= r0) & (u < r1)
         assert same((u[sel], v[sel], w[sel]), (wu, wv, ww))
+
+
+@pytest.mark.parametrize("nsym", [3, 6])
+def test_alphabets_against_oracle(ctx, orc, nsym):
+    """Families over 3 symbols (exact 4-gram filter, bins unused) and 6 symbols (hashed
+    3-gram filter, bit-vector verification) against the oracle."""
+    rng = np.random.default_rng(40 + nsym)
+    letters = np.frombuffer(b"QRSTUVWX"[:nsym], np.uint8)
+    seqs = []
+    for _ in range(50):
+        base = letters[rng.integers(0, nsym, size=int(rng.integers(60, 110)))]
+        for _ in range(20):
+            s = base.copy()
+            for _ in range(int(rng.integers(0, 6))):
+                p = int(rng.integers(0, s.size))
+                op = int(rng.integers(0, 3))
+                if op == 0:
+                    s[p] = letters[rng.integers(0, nsym)]
+                elif op == 1:
+                    s = np.insert(s, p, letters[rng.integers(0, nsym)])
+                elif s.size > 1:
+                    s = np.delete(s, p)
+            seqs.append(s.tobytes())
+    atoms = np.frombuffer(b"".join(seqs), np.uint8)
+    offsets = np.zeros(len(seqs) + 1, np.int64)
+    np.cumsum([len(s) for s in seqs], out=offsets[1:])
+    for r in (2.0, 6.0):
+        want = orc.eps_graph_edit(atoms, offsets, np.float32(r))
+        got = ctx.eps_graph_edit((atoms, offsets), np.float32(r))
+        assert same(got, want) and got[0].size > 0

@@ -100,3 +100,14 @@ def test_alphabets_against_oracle(ctx, orc, nsym):
         want = orc.eps_graph_edit(atoms, offsets, np.float32(r))
         got = ctx.eps_graph_edit((atoms, offsets), np.float32(r))
         assert same(got, want) and got[0].size > 0
+
+
+def test_short_strings_exact_filter(ctx, orc):
+    """Strings shorter than the filter's 4-grams over a DNA alphabet (no q-grams: the
+    filter passes them all, verification decides)."""
+    seqs = [b"", b"A", b"AC", b"ACG", b"ACGT", b"ACGTA", b"TTT", b"GA", b"", b"CCCC", b"ACGTACGT"] * 13
+    atoms = np.frombuffer(b"".join(seqs), np.uint8)
+    offsets = np.zeros(len(seqs) + 1, np.int64)
+    np.cumsum([len(s) for s in seqs], out=offsets[1:])
+    for r in (0.0, 1.0, 3.0):
+        assert same(ctx.eps_graph_edit((atoms, offsets), np.float32(r)), orc.eps_graph_edit(atoms, offsets, np.float32(r)))

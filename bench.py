@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="points of the descriptor workload (smaller sizes are for ncu captures only)")
+    ap.add_argument("--k5-points", type=int, default=5_000_000,
+                    help="points of the K5 workload (smaller sizes are for ncu captures only)")
     ap.add_argument("--workload", default="k2", choices=["k1", "k2", "k3", "k4", "k5"],
                     help="k2 (default) is the headline; k1, k3, k4, k5 print the same line for the other "
                          "configurations (see SECONDARY)")
@@ -339,7 +341,7 @@ def run_secondary(args, world, rank, local):
     wl = args.workload
     cfg = {}
     if wl in ("k1", "k5"):
-        x = synth.l2_mixture() if wl == "k1" else synth.zipf_mixture()
+        x = synth.l2_mixture() if wl == "k1" else synth.zipf_mixture(n=args.k5_points)
         radius = synth.EPS_K1 if wl == "k1" else synth.EPS_K5
         n, d = x.shape
         xd = torch.from_numpy(x).to(dev)

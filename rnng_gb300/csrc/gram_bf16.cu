@@ -657,14 +657,24 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 const int r0 = rb + 16 * hh;
                 uint32_t msk = 0;
                 if (mine) {
+                    // all 2 rows x 16 columns real and off the diagonal tile: the test alone
+                    if (!diag && r0 + 8 < n32 && cb + 57 < n32) {
 #pragma unroll
-                    for (int x = 0; x < 32; ++x) {
-                        const int gi = r0 + 8 * ((x >> 1) & 1);
-                        const int gj = cb + 8 * (x >> 2) + (x & 1);
-                        // padding rows / columns and, inside a diagonal tile, j <= i excluded
-                        const float term = FOLD ? -2.f * g[x] : g[x];
-                        const bool ok = term <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
-                        msk |= (ok ? 1u : 0u) << x;
+                        for (int x = 0; x < 32; ++x) {
+                            const float term = FOLD ? -2.f * g[x] : g[x];
+                            msk |= (term <= ((x & 2) ? W1 : W0) ? 1u : 0u) << x;
+                        }
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < 32; ++x) {
+                            const int gi = r0 + 8 * ((x >> 1) & 1);
+                            const int gj = cb + 8 * (x >> 2) + (x & 1);
+                            // padding rows / columns and, inside a diagonal tile, j <= i excluded
+                            const float term = FOLD ? -2.f * g[x] : g[x];
+                            const bool ok =
+                                term <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
+                            msk |= (ok ? 1u : 0u) << x;
+                        }
                     }
                 }
                 const int cnt = __popc(msk);

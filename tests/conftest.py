@@ -39,3 +39,18 @@ def golden_points(g):
     if "x" in g:
         return g["x"]
     return g["x_u8"].astype(np.float32)
+
+
+def colex_max_id(maxdim: int = 2) -> int:
+    """Largest vertex id for which every simplex id up to maxdim is an exact binomial sum
+    below the dimension bits (RNNG's Binom: a 64-bit falling product, signed division);
+    up to it the library generates simplices in id order."""
+    from math import comb, perm
+
+    def exact(m):
+        return all(perm(m, k) < 2 ** 63 and comb(m + 1, k) <= 2 ** 60 for k in range(1, maxdim + 2))
+    lo, hi = 0, 1 << 40
+    while lo < hi:
+        mid = (lo + hi + 1) // 2
+        lo, hi = (mid, hi) if exact(mid) else (lo, mid - 1)
+    return lo

@@ -3,7 +3,7 @@
 import numpy as np
 import pytest
 
-from conftest import golden
+from conftest import colex_max_id, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -116,20 +116,6 @@ def test_random_against_oracle(ctx, orc, maxdim):
     u, v, w = orc.eps_graph_l2(x, r)
     want = orc.rips(x.shape[0], u, v, w, maxdim)
     assert same(ctx.rips_l2(x, r, maxdim=maxdim), want)
-
-
-def colex_max_id(maxdim: int = 2) -> int:
-    """Largest vertex id for which every simplex id up to maxdim is an exact binomial sum
-    below the dimension bits (the library then builds simplices in id order)."""
-    from math import comb, perm
-
-    def exact(m):
-        return all(perm(m, k) < 2 ** 63 and comb(m + 1, k) <= 2 ** 60 for k in range(1, maxdim + 2))
-    lo, hi = 0, 1 << 40
-    while lo < hi:
-        mid = (lo + hi + 1) // 2
-        lo, hi = (mid, hi) if exact(mid) else (lo, mid - 1)
-    return lo
 
 
 def brute_filtration(orc, x, r, labels):

@@ -115,7 +115,10 @@ int rnng_ctx_trim(rnng_ctx* ctx);
  * VoronoiDiagram + add_ghost_points_systolic + per-cell radius_query_batched
  * (drivers/landmark.cpp:139-210, include/point.hpp:537-929, include/search.hpp:267-340).
  * X is n x d row-major float32; ids (may be NULL = 0..n-1) are the point ids.
- * Output: every unordered pair with L2 <= radius, as u < v (ids compared), each once. */
+ * Output: every unordered pair with L2 <= radius, as u < v (ids compared), each once.
+ * A point with a NaN or infinite coordinate is at L2 NaN or +inf from every point, so
+ * it has no edge (RNNG's own result for NaN rows); with radius = +inf such points
+ * would pair at distance +inf, which is refused with RNNG_ERR_UNSUPPORTED. */
 int rnng_eps_graph_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
                       int mode, unsigned flags, rnng_edges* out);
 
@@ -155,7 +158,8 @@ int rnng_eps_graph_edit(rnng_ctx* ctx, const uint8_t* atoms, const int64_t* offs
  * all vertices (value 0), edges (value = L2) and every clique of up to maxdim + 1
  * vertices (value = its largest edge, RNNG's max over facets), ids per
  * include/simplex.hpp:5-19 over the point ids, sorted by (value, id).  maxdim is 0..15
- * (the id keeps the dimension in 4 bits); RNNG's rips driver defaults to 3. */
+ * (the id keeps the dimension in 4 bits); RNNG's rips driver defaults to 3.  Points
+ * with a NaN or infinite coordinate are vertices without edges (as in rnng_eps_graph_l2). */
 int rnng_rips_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
                  int maxdim, int mode, unsigned flags, rnng_simplices* out);
 

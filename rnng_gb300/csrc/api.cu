@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <limits>
 #include <new>
 
 #include "common.cuh"
@@ -77,11 +78,30 @@ namespace rnng {
 
 // The L2 epsilon-graph pipeline on device-resident points (n >= 2, radius >= 0):
 // partition, covers, pruning, tiles.  Edges stay in sorted-index space in E; the
-// context events 2..5 (and 8..10 in BF16 mode) mark the stages.
+// context events 2..5 (and 8..10 in BF16 mode) mark the stages.  Rows with a NaN or
+// infinite coordinate get no edges (RNNG_ERR_UNSUPPORTED if the radius is +inf).
 int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, int mode, Layout& L, EdgeOut& E)
 {
     cudaStream_t s = c->stream;
-    L = build_layout(c, dX, n, d, radius);
+    L = build_layout(c, dX, n, d, radius, true);
+    int64_t n_in = n;
+    bool remap = false;
+    if (L.nonfinite) {
+        // rows with a NaN or infinite coordinate have no edge under a finite radius: the
+        // graph of the finite rows, mapped back to input rows at the end
+        const float* Xf = dX;
+        n = compact_finite_rows(c, dX, n_in, d, &Xf);
+        remap = n < n_in;
+        RNNG_REQUIRE(!remap || radius < std::numeric_limits<float>::infinity(), RNNG_ERR_UNSUPPORTED,
+                     "non-finite coordinates with an infinite radius");
+        if (n < 2) {
+            L = Layout{};
+            L.d = d;
+            for (int e : {2, 3, 4, 8, 5}) RNNG_CUDA(cudaEventRecord(c->ev[e], s));
+            return 0;
+        }
+        L = build_layout(c, Xf, n, d, radius, false);
+    }
     RNNG_CUDA(cudaEventRecord(c->ev[2], s));
     build_covers(c, L);
     RNNG_CUDA(cudaEventRecord(c->ev[3], s));
@@ -92,6 +112,7 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
         prepare_bf16(c, L);
     }
     const int64_t m = tiles_with_retry(c, L, mode, E);
+    if (remap) remap_rows(c, L.perm, n, n_in);
     RNNG_CUDA(cudaEventRecord(c->ev[5], s));
     return m;
 }
@@ -171,7 +192,7 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
                           &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
                           &c->items, &c->items_tmp, &c->sched_tmp, &c->sym, &c->shift_buf, &c->ball_b16,
-                          &c->ball_info, &c->lm_b16, &c->xb_sortedB};
+                          &c->ball_info, &c->lm_b16, &c->xb_sortedB, &c->fin_x, &c->fin_idx};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

@@ -36,8 +36,9 @@ struct Error {
 
 // Slots of the context's 64-bit device counter array (counters): 0-1 pruning, 2-3 edit counts,
 // 4 edges, 5 candidates, 6 query hits, 9 edit maximum length, 10-11 rips checks,
-// 12 ball widening (two floats).
+// 12 ball widening (two floats), 13 non-finite input seen.
 constexpr int kCounterSlots = 16;
+constexpr int kSlotNonfinite = 13;
 
 // A growable device buffer owned by the context.  Buffers are reused across calls
 // so that steady-state calls do not allocate.
@@ -86,7 +87,8 @@ struct rnng_ctx {
     rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
         out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched, clq0, clq1,
-        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info, lm_b16, xb_sortedB;
+        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info, lm_b16, xb_sortedB,
+        fin_x, fin_idx;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;
     int64_t last_candidates = 0;
@@ -158,6 +160,9 @@ __device__ __forceinline__ float l2seq_acc(float acc, float a, float b)
     float d = __fsub_rn(a, b);
     return __fadd_rn(acc, __fmul_rn(d, d));
 }
+
+// NaN or +-infinity: every exponent bit set.
+__device__ __forceinline__ bool nonfinite_f32(float v) { return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u; }
 
 // Warp-level tensor-core product c += A B (mma.sync m16n8k16, BF16 operands, FP32
 // accumulator) on the standard fragments: a0..a3 = A rows (g, g + 8) x k-slots

@@ -240,6 +240,58 @@ __global__ void k_iota_keys(int32_t* __restrict__ order, uint64_t* __restrict__ 
 }
 
 // ------------------------------------------------------------------------------------------------
+// non-finite rows
+//
+// A row with a NaN or infinite coordinate has an L2seq of NaN or +inf to every row
+// (x - y is NaN or infinite in that coordinate, and so is the sum of squares), so
+// under a finite radius it has no edge, as in RNNG's own paths (whose edge test is
+// dist <= radius, include/search.hpp:390-407).  Such rows would also poison the
+// partition's distances and the covering balls of their tile, so the graph is built
+// over the finite rows only and mapped back.
+
+// *flag = 1 if any of X[0..count) is NaN or infinite (flag zeroed by the caller).
+__global__ void k_any_nonfinite(const float* __restrict__ X, int64_t count, unsigned long long* __restrict__ flag)
+{
+    bool bad = false;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        bad |= nonfinite_f32(X[i]);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) *flag = 1ull;
+}
+
+// keep[r] = 1 if row r is finite, else 0; one warp per row.
+__global__ void k_row_finite(const float* __restrict__ X, int64_t n, int d, int32_t* __restrict__ keep)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        bool bad = false;
+        for (int k = lane; k < d; k += 32) bad |= nonfinite_f32(X[r * d + k]);
+        bad = __any_sync(0xffffffffu, bad);
+        if (lane == 0) keep[r] = bad ? 0 : 1;
+    }
+}
+
+// Finite row r to row pos[r] of Xc; map[pos[r]] = r.
+__global__ void k_compact_rows(const float* __restrict__ X, int64_t n, int d, const int32_t* __restrict__ keep,
+                               const int32_t* __restrict__ pos, float* __restrict__ Xc, int32_t* __restrict__ map)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        if (!keep[r]) continue;
+        const int64_t p = pos[r];
+        for (int k = lane; k < d; k += 32) Xc[p * d + k] = X[r * d + k];
+        if (lane == 0) map[p] = (int32_t)r;
+    }
+}
+
+__global__ void k_remap(int32_t* __restrict__ perm, int64_t n, const int32_t* __restrict__ map)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        perm[i] = map[perm[i]];
+}
+
+// ------------------------------------------------------------------------------------------------
 // host side
 
 void exclusive_scan_i32(rnng_ctx* c, const int32_t* in, int32_t* out, int64_t count)
@@ -261,6 +313,34 @@ static int grid_for(rnng_ctx* c, int64_t work, int per_block, int waves = 8)
     return (int)g;
 }
 
+int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out)
+{
+    cudaStream_t s = c->stream;
+    c->fin_idx.reserve(sizeof(int32_t) * (size_t)(3 * n + 2));
+    int32_t* keep = c->fin_idx.as<int32_t>();  // n + 1 (the scan's trailing slot)
+    int32_t* pos = keep + (n + 1);              // n + 1
+    int32_t* map = pos + (n + 1);               // n
+    k_row_finite<<<grid_for(c, n * 32, 256), 256, 0, s>>>(dX, n, d, keep); ++c->launches;
+    exclusive_scan_i32(c, keep, pos, n + 1);
+    int32_t nf = 0;
+    RNNG_CUDA(cudaMemcpyAsync(&nf, pos + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    RNNG_CUDA(cudaStreamSynchronize(s));
+    *out = dX;
+    if (nf == n) return n;
+    c->fin_x.reserve(sizeof(float) * (size_t)std::max<int64_t>(nf, 1) * d);
+    k_compact_rows<<<grid_for(c, n * 32, 256), 256, 0, s>>>(dX, n, d, keep, pos, c->fin_x.as<float>(), map);
+    ++c->launches;
+    *out = c->fin_x.as<float>();
+    return nf;
+}
+
+void remap_rows(rnng_ctx* c, int32_t* perm, int64_t n, int64_t n_in)
+{
+    if (n == 0) return;
+    const int32_t* map = c->fin_idx.as<int32_t>() + 2 * (n_in + 1);
+    k_remap<<<grid_for(c, n, 256), 256, 0, c->stream>>>(perm, n, map); ++c->launches;
+}
+
 void sort_pairs_u64(rnng_ctx* c, uint64_t* keys_in, uint64_t* keys_out, int32_t* vals_in, int32_t* vals_out,
                     int64_t n, int end_bit, int begin_bit)
 {
@@ -280,7 +360,7 @@ static int bits_for(int64_t v)
     return b;
 }
 
-Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius)
+Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, bool screen)
 {
     Layout L;
     L.n = n;
@@ -308,8 +388,19 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     int32_t* cend = cstart + cap;
     int32_t* nchild = cend + cap;
     int32_t* child_off = nchild + cap;
-    // BF16 shift (d <= 256): the assignment's distances come from the tensor cores
-    const float* shift = bf16_supported(d) ? bf16_shift(c, L, dX) : nullptr;
+    // non-finite screen: its flag is read with the first level's synchronisation
+    unsigned long long* nonfinite = nullptr;
+    if (screen) {
+        c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
+        nonfinite = c->counters.as<unsigned long long>() + kSlotNonfinite;
+        if (!bf16_supported(d)) {
+            RNNG_CUDA(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned long long), s));
+            k_any_nonfinite<<<grid_for(c, n * d, 1024), 256, 0, s>>>(dX, n * d, nonfinite); ++c->launches;
+        }
+    }
+    // BF16 shift (d <= 256): the assignment's distances come from the tensor cores; the
+    // column sums behind it read every value, so they carry the screen
+    const float* shift = bf16_supported(d) ? bf16_shift(c, L, dX, nonfinite) : nullptr;
     int levels = 0;
     for (; levels < kMaxLevels; ++levels) {
         // a cell can be empty (its landmark's point went to a sibling with an equal or, in the
@@ -321,7 +412,14 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         exclusive_scan_i32(c, nchild, child_off, ncells + 1);
         int32_t total = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, child_off + ncells, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        unsigned long long seen = 0;
+        if (levels == 0 && nonfinite)
+            RNNG_CUDA(cudaMemcpyAsync(&seen, nonfinite, sizeof(seen), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
+        if (seen) {
+            L.nonfinite = true;
+            return L;
+        }
         if (total == ncells) break;  // every cell is a leaf
         c->aux3.reserve(sizeof(int32_t) * (size_t)total);
         c->aux4.reserve(sizeof(float) * (size_t)total * d);

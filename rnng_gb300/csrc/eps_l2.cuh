@@ -35,6 +35,8 @@ struct Layout {
     int item_tiles = 1;
     unsigned long long* sched = nullptr;
     int sched_G = 0;
+    // build_layout stopped before the partition: the screen found a non-finite input value
+    bool nonfinite = false;
 };
 
 // Edge buffer in sorted-index space.
@@ -46,7 +48,16 @@ struct EdgeOut {
     unsigned long long cap = 0;
 };
 
-Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius);
+// screen: first test the input for NaN or infinite values (fused into the BF16 column
+// sums for d <= 256) and, if there is one, return at once with L.nonfinite set.
+Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, bool screen);
+// Rows of dX (n x d) without a NaN or infinite coordinate, copied in order to a context
+// buffer (*out; dX itself when every row is finite); returns their number.  The map
+// from compacted rows to input rows stays in the context for remap_rows.
+int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out);
+// perm[0..n) := map[perm[k]] with the map of the last compact_finite_rows (n_in: the
+// row count that call was given).
+void remap_rows(rnng_ctx* c, int32_t* perm, int64_t n, int64_t n_in);
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E);
 void finalize_edges(rnng_ctx* c, const Layout& L, const int64_t* d_ids, const EdgeOut& E, int64_t m, int64_t* u,
                     int64_t* v, float* w);
@@ -65,7 +76,8 @@ void prepare_bf16(rnng_ctx* c, Layout& L);
 double bf16_gamma(int d);
 // The BF16 shift of this layout: the rounded column means of the L.n points X (by
 // default L.Xs; the input rows give the same sums), computed once per call (L.shift).
-const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X = nullptr);
+// nonfinite (optional, device): set to 1 if a value of X is NaN or infinite, else 0.
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X = nullptr, unsigned long long* nonfinite = nullptr);
 // Ball centres (nb rows of L.d floats, radii rad; rows nb .. nb_pad - 1 padding) as BF16
 // rows of dp = 64 * ceil(d / 64) with {norm, a, q, radius or -1} per row (bf16_row).
 // Returns the mean relative widening of a ball pair's squared threshold by a and q.

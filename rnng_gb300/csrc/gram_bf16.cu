@@ -868,7 +868,9 @@ __global__ void __launch_bounds__(32 * kRecheckWarps) k_recheck(const float* __r
 // Per-dimension column sums (double) of the real rows, d <= 256: a block step covers
 // 256 / d whole rows as one contiguous run of floats, so thread t always adds dimension
 // t % d; per-thread float partials, then one double atomic per dimension and block.
-__global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, int64_t n, int d, double* __restrict__ sums)
+// nonfinite (optional, zeroed by the caller): set to 1 if a value is NaN or infinite.
+__global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, int64_t n, int d, double* __restrict__ sums,
+                                                unsigned long long* __restrict__ nonfinite)
 {
     __shared__ float part[256];
     const int rpb = 256 / d;  // rows per step
@@ -877,10 +879,15 @@ __global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, in
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
     float acc = 0.f;
+    bool bad = false;
     if (active)
-        for (int64_t r = r0 + t / d; r < r1; r += rpb) acc += Xs[r * d + t % d];
+        for (int64_t r = r0 + t / d; r < r1; r += rpb) {
+            const float v = Xs[r * d + t % d];
+            bad |= nonfinite_f32(v);
+            acc += v;
+        }
     part[t] = acc;
-    __syncthreads();
+    if (__syncthreads_or(bad) && nonfinite && t == 0) *nonfinite = 1ull;
     if (t < d) {
         double s2 = 0.0;
         for (int q = 0; q < rpb; ++q) s2 += (double)part[q * d + t];
@@ -888,9 +895,16 @@ __global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, in
     }
 }
 
+// Rounded column means.  A non-finite column sum (a NaN or infinite coordinate, or a
+// float partial that overflowed) gets shift 0: any finite shift keeps the BF16 error
+// bounds valid.
 __global__ void k_shift(const double* __restrict__ sums, int64_t n, int d, float* __restrict__ shift)
 {
-    for (int k = threadIdx.x; k < d; k += blockDim.x) shift[k] = (float)rint(sums[k] / (double)(n > 0 ? n : 1));
+    for (int k = threadIdx.x; k < d; k += blockDim.x) {
+        const double s = sums[k];
+        const bool fin = (__double_as_longlong(s) & 0x7ff0000000000000ll) != 0x7ff0000000000000ll;
+        shift[k] = fin ? (float)rint(s / (double)(n > 0 ? n : 1)) : 0.f;
+    }
 }
 
 // One warp: the BF16 row of x (d floats; zeros when !real) shifted by `shift` and zero
@@ -1055,7 +1069,7 @@ double bf16_gamma(int d)
     return (double)dp * std::ldexp(1.0, -19) + (double)(d + 8) * std::ldexp(1.0, -24) + 2.0 * std::ldexp(1.0, -24);
 }
 
-const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X)
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X, unsigned long long* nonfinite)
 {
     if (L.shift) return L.shift;
     if (!X) X = L.Xs;
@@ -1066,7 +1080,8 @@ const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X)
     float* shift = (float*)(sums + d);
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 4));
-    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums); ++c->launches;
+    if (nonfinite) RNNG_CUDA(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned long long), s));
+    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums, nonfinite); ++c->launches;
     k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
     L.shift = shift;
     return shift;

@@ -7,7 +7,7 @@ the binary-dump harness oracle/ref_harness.cpp, which makes the same API calls a
 RNNG's drivers.  The expected outputs are stored with full float bits.
 
     make -C oracle ref            # needs the RNNG sources (REF=/path/to/RNNG)
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]   # default: all of them
 
 Fixtures (npz, inputs + expected):
   k1_systolic   L2 mixture, 3000 x 8, radius 1.5, systolic path (cover tree + ring)
@@ -24,6 +24,12 @@ Fixtures (npz, inputs + expected):
   k3_cells      the k3 strings' cells (30 landmarks) with the rips driver's ghosts
   dup_cells     400 points on 60 distinct positions in R^4, 40 landmarks: identical
                 landmarks leave cells empty
+  nan_systolic  L2 mixture, 2000 x 8, radius 3, with 45 rows holding NaN coordinates
+                (40 with one, 5 all NaN), systolic path: such rows get no edges;
+                nan_landmark the same input through the landmark path (20 landmarks)
+  nan_rips      torus in R^16, 400 points, 12 of them with a NaN coordinate, maxdim 2,
+                rips path: they stay vertices without edges
+  (RNNG's cover tree does not survive infinite coordinates, so no fixture has them.)
 Edge fixtures hold the unordered edge set (u < v) with weights, and the driver's
 reported edge count (n + 2|E|); the Rips fixtures hold the merged filtration; the cell
 fixtures hold per cell its id, point ids, distances to the centre, interior flags and
@@ -48,11 +54,30 @@ from rnng_gb300 import synth  # noqa: E402
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 
+ONLY = set(sys.argv[1:])
+
+
+def wanted(name):
+    return not ONLY or name in ONLY
+
+
+def with_nan_rows(x, ones, whole, seed):
+    """A copy of x with `ones` rows holding one NaN coordinate and `whole` rows all NaN."""
+    rng = np.random.default_rng(seed)
+    x = x.copy()
+    rows = rng.choice(x.shape[0], size=ones + whole, replace=False)
+    x[rows[:ones], rng.integers(0, x.shape[1], size=ones)] = np.nan
+    x[rows[ones:]] = np.nan
+    return x
+
+
 def run(args):
     subprocess.run([HARNESS] + [str(a) for a in args], check=True)
 
 
 def edges_fixture(name, tmp, mode, path_in, radius, extra, n, save_inputs):
+    if not wanted(name):
+        return
     out = os.path.join(tmp, name + ".bin")
     if mode == "systolic":
         run(["systolic", path_in, repr(float(radius)), out])
@@ -66,6 +91,8 @@ def edges_fixture(name, tmp, mode, path_in, radius, extra, n, save_inputs):
 
 
 def cells_fixture(name, tmp, metric, path_in, radius, m, seed, rips, save_inputs):
+    if not wanted(name):
+        return
     out = os.path.join(tmp, name + ".bin")
     run(["cells", metric, path_in, repr(float(radius)), m, seed, 1 if rips else 0, out])
     cells = oracle.read_cells_dump(out)
@@ -76,6 +103,8 @@ def cells_fixture(name, tmp, metric, path_in, radius, m, seed, rips, save_inputs
 
 
 def rips_fixture(name, tmp, metric, path_in, radius, maxdim, m, seed, n, save_inputs):
+    if not wanted(name):
+        return
     out = os.path.join(tmp, name + ".bin")
     run(["rips", metric, path_in, repr(float(radius)), maxdim, m, seed, out])
     ids, vals = oracle.read_simplex_dump(out)
@@ -150,6 +179,19 @@ def main():
         pd = os.path.join(tmp, "dup.fvecs")
         synth.write_fvecs(pd, xd)
         cells_fixture("dup_cells", tmp, "l2", pd, np.float32(3.0), 40, 11, True, {"x": xd})
+
+        # rows with NaN coordinates
+        xn = with_nan_rows(synth.l2_mixture(n=2000, d=8, k=16, seed=21), 40, 5, 21)
+        pn = os.path.join(tmp, "nan.fvecs")
+        synth.write_fvecs(pn, xn)
+        edges_fixture("nan_systolic", tmp, "systolic", pn, np.float32(3.0), None, 2000, {"x": xn})
+        edges_fixture("nan_landmark", tmp, "l2", pn, np.float32(3.0), ("20", "7"), 2000, {"x": xn})
+        xt = synth.torus16(n=400, seed=22)
+        er = synth.choose_eps(xt, 12.0, sample=400)
+        xr = with_nan_rows(xt, 12, 0, 22)
+        pr = os.path.join(tmp, "nanr.fvecs")
+        synth.write_fvecs(pr, xr)
+        rips_fixture("nan_rips", tmp, "l2", pr, er, 2, 10, 7, 400, {"x": xr})
 
 if __name__ == "__main__":
     main()

@@ -49,15 +49,17 @@ def assert_edges(orc, dump, g):
     assert full == int(g["reported_edges"])
 
 
-def test_systolic_k1(harness, orc, tmp_path):
-    g = golden("k1_systolic")
+@pytest.mark.parametrize("name", ["k1_systolic", "nan_systolic"])
+def test_systolic(harness, orc, tmp_path, name):
+    g = golden(name)
     _, path = write_input(tmp_path, g)
     out = str(tmp_path / "out.bin")
     run(harness, "systolic", path, repr(float(g["radius"])), out)
     assert_edges(orc, out, g)
 
 
-@pytest.mark.parametrize("name,m", [("k1_landmark", 30), ("k2_landmark", 12), ("k3_edit", 30), ("k5_landmark", 40)])
+@pytest.mark.parametrize("name,m", [("k1_landmark", 30), ("k2_landmark", 12), ("k3_edit", 30), ("k5_landmark", 40),
+                                    ("nan_landmark", 20)])
 def test_landmark(harness, orc, tmp_path, name, m):
     g = golden(name)
     metric, path = write_input(tmp_path, g)
@@ -77,7 +79,7 @@ def test_cells_and_ghosts(harness, orc, tmp_path, name):
         assert np.array_equal(got[k], g[k]), k
 
 
-@pytest.mark.parametrize("name,m", [("k4_rips", 24), ("k4_rips3", 12), ("k3_rips_edit", 10)])
+@pytest.mark.parametrize("name,m", [("k4_rips", 24), ("k4_rips3", 12), ("k3_rips_edit", 10), ("nan_rips", 10)])
 def test_rips(harness, orc, tmp_path, name, m):
     g = golden(name)
     metric, path = write_input(tmp_path, g)

@@ -16,7 +16,7 @@ def same(a, b):
 
 
 @pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("name", ["k1_systolic", "k2_landmark", "k5_landmark"])
+@pytest.mark.parametrize("name", ["k1_systolic", "k2_landmark", "k5_landmark", "nan_systolic"])
 def test_golden_fixture(ctx, mode, name):
     g = golden(name)
     got = ctx.eps_graph_l2(golden_points(g), g["radius"], mode=mode)
@@ -114,3 +114,49 @@ def test_both_pruning_paths_exact(ctx, orc, mode):
         st = ctx.stats()
         assert st["prune_tensor"] == tensor, st["prune_widen"]
         assert same(got, orc.eps_graph_l2(x, r)) and got[0].size > 0
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("d", [8, 100, 300])
+def test_nonfinite_rows(ctx, orc, mode, d):
+    """Rows with a NaN or infinite coordinate get no edges and leave every other edge in
+    place (RNNG's dist <= radius is false for them); NaN, +inf and -inf, single
+    coordinates and whole rows, in every tile position."""
+    import rnng_gb300
+    if mode == "bf16" and d > 256:
+        pytest.skip("BF16 mode supports d <= 256")
+    rng = np.random.default_rng(d)
+    n = 3000
+    centres = rng.uniform(-6, 6, size=(10, d))
+    x = (centres[rng.integers(0, 10, n)] + rng.normal(size=(n, d))).astype(np.float32)
+    r = np.float32(np.sqrt(2.0 * d) * 0.9)
+    bad = rng.choice(n, size=90, replace=False)
+    vals = np.array([np.nan, np.inf, -np.inf], np.float32)
+    x[bad[:60], rng.integers(0, d, size=60)] = vals[np.arange(60) % 3]
+    x[bad[60:75]] = np.nan
+    x[bad[75:], :] = np.inf
+    want = orc.eps_graph_l2(x, r)
+    assert want[0].size > 1000
+    got = ctx.eps_graph_l2(x, r, mode=mode)
+    assert same(got, want)
+    assert not np.isin(got[0], bad).any() and not np.isin(got[1], bad).any()
+    # through the Rips entry point: non-finite rows stay vertices without edges
+    ids, vals_ = ctx.rips_l2(x[:800], r, maxdim=1, mode=mode)
+    u, v, w = orc.eps_graph_l2(x[:800], r)
+    wi, wv = orc.rips(800, u, v, w, 1)
+    assert np.array_equal(ids, wi) and np.array_equal(vals_.view(np.uint32), wv.view(np.uint32))
+    # all rows but one, and all rows, non-finite
+    y = np.full((500, d), np.nan, np.float32)
+    assert ctx.eps_graph_l2(y, r, mode=mode)[0].size == 0
+    y[7] = 0.0
+    assert ctx.eps_graph_l2(y, r, mode=mode)[0].size == 0
+    y[300] = 0.0
+    u, v, w = ctx.eps_graph_l2(y, r, mode=mode)
+    assert u.tolist() == [7] and v.tolist() == [300] and w.tolist() == [0.0]
+    # an infinite radius would admit pairs at distance +inf: refused, not guessed
+    with pytest.raises(rnng_gb300.RnngError) as e:
+        ctx.eps_graph_l2(x, np.float32(np.inf), mode=mode)
+    assert e.value.code == 6
+    # the context stays usable and finite inputs take the unscreened path again
+    z = x[np.isfinite(x).all(axis=1)]
+    assert same(ctx.eps_graph_l2(z, r, mode=mode), orc.eps_graph_l2(z, r))

@@ -39,6 +39,29 @@ def test_voronoi_matches_reference_rule(ctx, orc, m):
     assert np.array_equal(cell, wc) and np.array_equal(dist.view(np.uint32), wd.view(np.uint32))
 
 
+def test_nonfinite_points_and_centres(ctx, orc):
+    """NaN and infinite coordinates: a query or point with one matches nothing, a
+    point whose distances are all NaN keeps cell 0 at FLT_MAX (the reference's initial
+    best), and a NaN centre is never nearest - as in RNNG's loops."""
+    rng = np.random.default_rng(41)
+    x = rng.normal(size=(2000, 9)).astype(np.float32)
+    q = rng.normal(size=(500, 9)).astype(np.float32)
+    x[rng.choice(2000, 50, replace=False), rng.integers(0, 9, 50)] = np.nan
+    x[rng.choice(2000, 20, replace=False), rng.integers(0, 9, 20)] = -np.inf
+    q[rng.choice(500, 30, replace=False), rng.integers(0, 9, 30)] = np.inf
+    want = orc.cross_l2(x, q, np.float32(2.5))
+    got = ctx.radius_query_l2(x, q, np.float32(2.5))
+    assert all(np.array_equal(a, b) for a, b in zip(got[:2], want[:2])) and want[0].size > 1000
+    assert np.array_equal(got[2].view(np.uint32), want[2].view(np.uint32))
+    c = x[::97].copy()
+    c[3] = np.nan
+    c[5, 2] = np.inf
+    cell, dist = ctx.voronoi_l2(x, c)
+    wc, wd = orc.voronoi(x, c)
+    assert np.array_equal(cell, wc) and np.array_equal(dist.view(np.uint32), wd.view(np.uint32))
+    assert not np.any(cell == 3)
+
+
 def test_voronoi_ties_go_to_the_last_centre(ctx):
     x = np.zeros((5, 3), np.float32)
     c = np.zeros((4, 3), np.float32)  # four identical centres: every point ties

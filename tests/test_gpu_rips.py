@@ -21,6 +21,14 @@ def test_golden_k4(ctx, mode):
 
 
 @pytest.mark.parametrize("mode", ["fp32", "bf16"])
+def test_golden_nan_rows(ctx, mode):
+    """Points with NaN coordinates are vertices without edges, as in RNNG's rips path."""
+    g = golden("nan_rips")
+    got = ctx.rips_l2(g["x"], g["radius"], maxdim=int(g["maxdim"]), mode=mode)
+    assert same(got, (g["ids"], g["values"]))
+
+
+@pytest.mark.parametrize("mode", ["fp32", "bf16"])
 def test_golden_k4_maxdim3(ctx, mode):
     """The rips driver's default dimension (tetrahedra) against RNNG's own output."""
     g = golden("k4_rips3")

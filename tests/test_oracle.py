@@ -9,7 +9,7 @@ import pytest
 
 from conftest import ROOT, golden, golden_points
 
-EDGE_FIXTURES = ["k1_systolic", "k1_landmark", "k2_landmark", "k5_landmark"]
+EDGE_FIXTURES = ["k1_systolic", "k1_landmark", "k2_landmark", "k5_landmark", "nan_systolic", "nan_landmark"]
 
 
 @pytest.mark.parametrize("name", EDGE_FIXTURES)
@@ -19,8 +19,9 @@ def test_oracle_l2_matches_reference(orc, name):
     u, v, w = orc.eps_graph_l2(x, g["radius"])
     assert np.array_equal(u, g["u"]) and np.array_equal(v, g["v"])
     assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
-    # the driver's printed count is n + 2|E| (self-loops and both orientations)
-    assert int(g["reported_edges"]) == int(g["n"]) + 2 * u.size
+    # the driver's printed count is its self-loops plus both orientations of every edge;
+    # a row with a NaN coordinate is at distance NaN from itself and has no self-loop
+    assert int(g["reported_edges"]) == int(np.isfinite(x).all(axis=1).sum()) + 2 * u.size
 
 
 def test_oracle_edit_matches_reference(orc):
@@ -31,7 +32,7 @@ def test_oracle_edit_matches_reference(orc):
     assert int(g["reported_edges"]) == int(g["n"]) + 2 * u.size
 
 
-@pytest.mark.parametrize("name", ["k4_rips", "k4_rips3", "k3_rips_edit"])
+@pytest.mark.parametrize("name", ["k4_rips", "k4_rips3", "k3_rips_edit", "nan_rips"])
 def test_oracle_rips_matches_reference(orc, name):
     g = golden(name)
     if "atoms" in g:

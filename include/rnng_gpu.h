@@ -117,8 +117,9 @@ int rnng_ctx_trim(rnng_ctx* ctx);
  * X is n x d row-major float32; ids (may be NULL = 0..n-1) are the point ids.
  * Output: every unordered pair with L2 <= radius, as u < v (ids compared), each once.
  * A point with a NaN or infinite coordinate is at L2 NaN or +inf from every point, so
- * it has no edge (RNNG's own result for NaN rows); with radius = +inf such points
- * would pair at distance +inf, which is refused with RNNG_ERR_UNSUPPORTED. */
+ * it has no edge (RNNG's own result for NaN rows); with radius = +inf a point with an
+ * infinite coordinate and no NaN would pair at distance +inf, which is refused with
+ * RNNG_ERR_UNSUPPORTED. */
 int rnng_eps_graph_l2(rnng_ctx* ctx, const float* X, const int64_t* ids, int64_t n, int64_t d, float radius,
                       int mode, unsigned flags, rnng_edges* out);
 

@@ -79,7 +79,8 @@ namespace rnng {
 // The L2 epsilon-graph pipeline on device-resident points (n >= 2, radius >= 0):
 // partition, covers, pruning, tiles.  Edges stay in sorted-index space in E; the
 // context events 2..5 (and 8..10 in BF16 mode) mark the stages.  Rows with a NaN or
-// infinite coordinate get no edges (RNNG_ERR_UNSUPPORTED if the radius is +inf).
+// infinite coordinate get no edges (RNNG_ERR_UNSUPPORTED if the radius is +inf and a
+// row has an infinity without a NaN).
 int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, int mode, Layout& L, EdgeOut& E)
 {
     cudaStream_t s = c->stream;
@@ -89,11 +90,15 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
     if (L.nonfinite) {
         // rows with a NaN or infinite coordinate have no edge under a finite radius: the
         // graph of the finite rows, mapped back to input rows at the end
+        // (a row with a NaN is at L2 NaN from every row, so it has no edge at any radius;
+        // rows with infinities only are at +inf from some rows, which an infinite radius
+        // would admit)
         const float* Xf = dX;
-        n = compact_finite_rows(c, dX, n_in, d, &Xf);
+        bool inf_rows = false;
+        n = compact_finite_rows(c, dX, n_in, d, &Xf, &inf_rows);
         remap = n < n_in;
-        RNNG_REQUIRE(!remap || radius < std::numeric_limits<float>::infinity(), RNNG_ERR_UNSUPPORTED,
-                     "non-finite coordinates with an infinite radius");
+        RNNG_REQUIRE(!inf_rows || radius < std::numeric_limits<float>::infinity(), RNNG_ERR_UNSUPPORTED,
+                     "infinite coordinates with an infinite radius");
         if (n < 2) {
             L = Layout{};
             L.d = d;

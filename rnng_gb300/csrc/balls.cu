@@ -770,8 +770,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
     cudaStream_t s = c->stream;
     c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
     unsigned long long* cnt = c->counters.as<unsigned long long>();
-    const double u = 5.9604644775390625e-08;
-    const float eps_p = std::nextafter((float)((double)L.radius * (1.0 + (L.d + 8) * u) + 1e-30), INFINITY);
+    const float eps_p = widened_radius(L.radius, L.d);
     const float shrink = 1.f - L.relerr;
     // level 1: bitmap of close super-tile pairs
     const int64_t NB = L.S * kBalls;

@@ -23,6 +23,9 @@
 //   7. map sorted indices back to ids, order each edge as u < v
 #include <cub/cub.cuh>
 
+#include <cfloat>
+#include <cmath>
+
 #include "common.cuh"
 #include "eps_l2.cuh"
 #include "balls.cuh"
@@ -258,16 +261,27 @@ __global__ void k_any_nonfinite(const float* __restrict__ X, int64_t count, unsi
     if (__syncthreads_or(bad) && threadIdx.x == 0) *flag = 1ull;
 }
 
-// keep[r] = 1 if row r is finite, else 0; one warp per row.
-__global__ void k_row_finite(const float* __restrict__ X, int64_t n, int d, int32_t* __restrict__ keep)
+// keep[r] = 1 if row r is finite, else 0; one warp per row.  *inf_rows = 1 (zeroed by
+// the caller) if some row has an infinite coordinate and no NaN: such a row is at L2
+// +inf, not NaN, from the rows it shares no infinite coordinate with.
+__global__ void k_row_finite(const float* __restrict__ X, int64_t n, int d, int32_t* __restrict__ keep,
+                             unsigned long long* __restrict__ inf_rows)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        bool bad = false;
-        for (int k = lane; k < d; k += 32) bad |= nonfinite_f32(X[r * d + k]);
+        bool bad = false, nan = false;
+        for (int k = lane; k < d; k += 32) {
+            const float v = X[r * d + k];
+            bad |= nonfinite_f32(v);
+            nan |= (__float_as_uint(v) & 0x7fffffffu) > 0x7f800000u;
+        }
         bad = __any_sync(0xffffffffu, bad);
-        if (lane == 0) keep[r] = bad ? 0 : 1;
+        nan = __any_sync(0xffffffffu, nan);
+        if (lane == 0) {
+            keep[r] = bad ? 0 : 1;
+            if (bad && !nan) *inf_rows = 1ull;
+        }
     }
 }
 
@@ -313,18 +327,24 @@ static int grid_for(rnng_ctx* c, int64_t work, int per_block, int waves = 8)
     return (int)g;
 }
 
-int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out)
+int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out, bool* inf_rows)
 {
     cudaStream_t s = c->stream;
     c->fin_idx.reserve(sizeof(int32_t) * (size_t)(3 * n + 2));
     int32_t* keep = c->fin_idx.as<int32_t>();  // n + 1 (the scan's trailing slot)
     int32_t* pos = keep + (n + 1);              // n + 1
     int32_t* map = pos + (n + 1);               // n
-    k_row_finite<<<grid_for(c, n * 32, 256), 256, 0, s>>>(dX, n, d, keep); ++c->launches;
+    c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
+    unsigned long long* dinf = c->counters.as<unsigned long long>() + kSlotNonfinite;
+    RNNG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(unsigned long long), s));
+    k_row_finite<<<grid_for(c, n * 32, 256), 256, 0, s>>>(dX, n, d, keep, dinf); ++c->launches;
     exclusive_scan_i32(c, keep, pos, n + 1);
     int32_t nf = 0;
+    unsigned long long hinf = 0;
     RNNG_CUDA(cudaMemcpyAsync(&nf, pos + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    RNNG_CUDA(cudaMemcpyAsync(&hinf, dinf, sizeof(hinf), cudaMemcpyDeviceToHost, s));
     RNNG_CUDA(cudaStreamSynchronize(s));
+    *inf_rows = hinf != 0;
     *out = dX;
     if (nf == n) return n;
     c->fin_x.reserve(sizeof(float) * (size_t)std::max<int64_t>(nf, 1) * d);
@@ -448,6 +468,15 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     L.relerr = (float)((d + 16) * 1.1920928955078125e-07);  // (d+16) * 2^-23
     L.radius = radius;
     return L;
+}
+
+float widened_radius(float radius, int d)
+{
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    const double ep = (double)radius * (1.0 + (double)(d + 8) * u) + 1e-30;
+    if (!(ep < (double)FLT_MAX)) return FLT_MAX;
+    const float f = std::nextafter((float)ep, INFINITY);
+    return f <= FLT_MAX ? f : FLT_MAX;
 }
 
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E)

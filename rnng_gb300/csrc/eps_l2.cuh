@@ -53,11 +53,17 @@ struct EdgeOut {
 Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, bool screen);
 // Rows of dX (n x d) without a NaN or infinite coordinate, copied in order to a context
 // buffer (*out; dX itself when every row is finite); returns their number.  The map
-// from compacted rows to input rows stays in the context for remap_rows.
-int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out);
+// from compacted rows to input rows stays in the context for remap_rows.  *inf_rows:
+// some row has an infinite coordinate and no NaN.
+int64_t compact_finite_rows(rnng_ctx* c, const float* dX, int64_t n, int d, const float** out, bool* inf_rows);
 // perm[0..n) := map[perm[k]] with the map of the last compact_finite_rows (n_in: the
 // row count that call was given).
 void remap_rows(rnng_ctx* c, int32_t* perm, int64_t n, int64_t n_in);
+// The radius the covers and the BF16 candidate test use: radius (1 + (d + 8) 2^-24) +
+// 1e-30 rounded up to a float, which bounds the FP32 rounding of RNNG's sequential L2.
+// Capped at FLT_MAX: an infinite (or huge) radius then still makes every squared
+// threshold +inf, without the NaN of inf x 0 where a tile's error radius is 0.
+float widened_radius(float radius, int d);
 void run_tiles_fp32(rnng_ctx* c, Layout& L, EdgeOut& E);
 void finalize_edges(rnng_ctx* c, const Layout& L, const int64_t* d_ids, const EdgeOut& E, int64_t m, int64_t* u,
                     int64_t* v, float* w);

@@ -1116,7 +1116,6 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     float* ucol = (float*)(rowinfo + L.n_pad);
     float2* tileinfo = (float2*)(ucol + L.n_pad);
     const float* shift = bf16_shift(c, L);
-    const double u = std::ldexp(1.0, -24);
     // four free padding columns carry the column terms through the tensor cores
     c->bf16_fold = dp - d >= 4;
     if (c->bf16_fold) c->xb_sortedB.reserve(sizeof(__nv_bfloat16) * (size_t)L.n_pad * dp);
@@ -1131,8 +1130,7 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     static_assert(sizeof(CUtensorMap) == sizeof(c->tmap), "tensor map storage");
     c->bf16_dp = dp;
     c->bf16_rowinfo = rowinfo;
-    double ep = (double)L.radius * (1.0 + (double)(d + 8) * u) + 1e-30;
-    c->bf16_eps_p = std::nextafter((float)ep, INFINITY);
+    c->bf16_eps_p = widened_radius(L.radius, d);
 
     CUtensorMap& tm = *reinterpret_cast<CUtensorMap*>(c->tmap);
     cuuint64_t gdim[2] = {(cuuint64_t)dp, (cuuint64_t)L.n_pad};

@@ -157,6 +157,35 @@ def test_nonfinite_rows(ctx, orc, mode, d):
     with pytest.raises(rnng_gb300.RnngError) as e:
         ctx.eps_graph_l2(x, np.float32(np.inf), mode=mode)
     assert e.value.code == 6
+    # ... unless every non-finite row holds a NaN (at distance NaN from everything): then
+    # the graph is complete over the finite rows
+    y = x[:260].copy()
+    y[~np.isfinite(y).all(axis=1), 0] = np.nan
+    y[5, 1] = np.nan
+    want = orc.eps_graph_l2(y, np.float32(np.inf))
+    assert same(ctx.eps_graph_l2(y, np.float32(np.inf), mode=mode), want)
+    k = int(np.isfinite(y).all(axis=1).sum())
+    assert want[0].size == k * (k - 1) // 2
     # the context stays usable and finite inputs take the unscreened path again
     z = x[np.isfinite(x).all(axis=1)]
     assert same(ctx.eps_graph_l2(z, r, mode=mode), orc.eps_graph_l2(z, r))
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_unbounded_radius(ctx, orc, mode):
+    """radius +inf, FLT_MAX and 1e30 admit every pair, also for integer points that BF16
+    holds exactly (every tile's error radius 0, where an infinite threshold times 0
+    would be NaN)."""
+    rng = np.random.default_rng(77)
+    xi = rng.integers(0, 16, size=(300, 16)).astype(np.float32)
+    xf = rng.normal(size=(300, 16)).astype(np.float32)
+    for x in (xi, xf):
+        for r in (np.float32(np.inf), np.float32(np.finfo(np.float32).max), np.float32(1e30)):
+            want = orc.eps_graph_l2(x, r)
+            assert want[0].size == 300 * 299 // 2
+            assert same(ctx.eps_graph_l2(x, r, mode=mode), want)
+    ids, vals = ctx.rips_l2(xi[:60], np.float32(np.inf), maxdim=2, mode=mode)
+    u, v, w = orc.eps_graph_l2(xi[:60], np.float32(np.inf))
+    wi, wv = orc.rips(60, u, v, w, 2)
+    assert wi.size == 60 + 60 * 59 // 2 + 60 * 59 * 58 // 6
+    assert np.array_equal(ids, wi) and np.array_equal(vals.view(np.uint32), wv.view(np.uint32))

@@ -112,11 +112,16 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
     RNNG_CUDA(cudaEventRecord(c->ev[3], s));
     prune_covers(c, L);
     RNNG_CUDA(cudaEventRecord(c->ev[4], s));
-    if (mode == RNNG_MODE_BF16_RECHECK) {
+    // the BF16 candidate test needs its squared terms in FP32's normal range (coordinates
+    // up to about 2^61 / sqrt(d), a radius of at least 2^-40); beyond it the FP32-direct
+    // tiles evaluate the surviving tile pairs
+    const int tmode = (mode == RNNG_MODE_BF16_RECHECK && !bf16_in_range(L)) ? RNNG_MODE_FP32_DIRECT : mode;
+    if (tmode == RNNG_MODE_BF16_RECHECK) {
         schedule_items(c, L, c->num_sms, gram_item_tiles(L.d));
         prepare_bf16(c, L);
     }
-    const int64_t m = tiles_with_retry(c, L, mode, E);
+    const int64_t m = tiles_with_retry(c, L, tmode, E);
+    if (tmode != mode) RNNG_CUDA(cudaEventRecord(c->ev[8], s));
     if (remap) remap_rows(c, L.perm, n, n_in);
     RNNG_CUDA(cudaEventRecord(c->ev[5], s));
     return m;

@@ -36,7 +36,8 @@ struct Error {
 
 // Slots of the context's 64-bit device counter array (counters): 0-1 pruning, 2-3 edit counts,
 // 4 edges, 5 candidates, 6 query hits, 9 edit maximum length, 10-11 rips checks,
-// 12 ball widening (two floats), 13 non-finite input seen.
+// 12 ball widening (two floats), 13 non-finite input seen, 14 largest input magnitude
+// (float bits).
 constexpr int kCounterSlots = 16;
 constexpr int kSlotNonfinite = 13;
 

@@ -25,6 +25,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 #include "eps_l2.cuh"
@@ -408,19 +409,20 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
     int32_t* cend = cstart + cap;
     int32_t* nchild = cend + cap;
     int32_t* child_off = nchild + cap;
-    // non-finite screen: its flag is read with the first level's synchronisation
-    unsigned long long* nonfinite = nullptr;
-    if (screen) {
-        c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
-        nonfinite = c->counters.as<unsigned long long>() + kSlotNonfinite;
-        if (!bf16_supported(d)) {
-            RNNG_CUDA(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned long long), s));
-            k_any_nonfinite<<<grid_for(c, n * d, 1024), 256, 0, s>>>(dX, n * d, nonfinite); ++c->launches;
+    // input screen, read with the first level's synchronisation: a non-finite value seen
+    // and (d <= 256) the largest magnitude
+    c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
+    unsigned long long* scr = c->counters.as<unsigned long long>() + kSlotNonfinite;
+    const bool b16 = bf16_supported(d);
+    if (!b16) {
+        RNNG_CUDA(cudaMemsetAsync(scr, 0, sizeof(unsigned long long), s));
+        if (screen) {
+            k_any_nonfinite<<<grid_for(c, n * d, 1024), 256, 0, s>>>(dX, n * d, scr); ++c->launches;
         }
     }
     // BF16 shift (d <= 256): the assignment's distances come from the tensor cores; the
     // column sums behind it read every value, so they carry the screen
-    const float* shift = bf16_supported(d) ? bf16_shift(c, L, dX, nonfinite) : nullptr;
+    const float* shift = b16 ? bf16_shift(c, L, dX, scr) : nullptr;
     int levels = 0;
     for (; levels < kMaxLevels; ++levels) {
         // a cell can be empty (its landmark's point went to a sibling with an equal or, in the
@@ -432,13 +434,17 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         exclusive_scan_i32(c, nchild, child_off, ncells + 1);
         int32_t total = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, child_off + ncells, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        unsigned long long seen = 0;
-        if (levels == 0 && nonfinite)
-            RNNG_CUDA(cudaMemcpyAsync(&seen, nonfinite, sizeof(seen), cudaMemcpyDeviceToHost, s));
+        unsigned long long hs[2] = {0ull, 0ull};
+        if (levels == 0)
+            RNNG_CUDA(cudaMemcpyAsync(hs, scr, (b16 ? 2 : 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
-        if (seen) {
-            L.nonfinite = true;
-            return L;
+        if (levels == 0) {
+            if (screen && hs[0]) {
+                L.nonfinite = true;
+                return L;
+            }
+            const uint32_t bits = (uint32_t)hs[1];
+            std::memcpy(&L.maxabs, &bits, sizeof(float));
         }
         if (total == ncells) break;  // every cell is a leaf
         c->aux3.reserve(sizeof(int32_t) * (size_t)total);

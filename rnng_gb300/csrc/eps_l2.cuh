@@ -37,6 +37,7 @@ struct Layout {
     int sched_G = 0;
     // build_layout stopped before the partition: the screen found a non-finite input value
     bool nonfinite = false;
+    float maxabs = 0.f;  // largest |coordinate| (d <= 256 only)
 };
 
 // Edge buffer in sorted-index space.
@@ -49,7 +50,8 @@ struct EdgeOut {
 };
 
 // screen: first test the input for NaN or infinite values (fused into the BF16 column
-// sums for d <= 256) and, if there is one, return at once with L.nonfinite set.
+// sums for d <= 256) and, if there is one, return at once with L.nonfinite set.  For
+// d <= 256 L.maxabs is set either way.
 Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, bool screen);
 // Rows of dX (n x d) without a NaN or infinite coordinate, copied in order to a context
 // buffer (*out; dX itself when every row is finite); returns their number.  The map
@@ -82,8 +84,12 @@ void prepare_bf16(rnng_ctx* c, Layout& L);
 double bf16_gamma(int d);
 // The BF16 shift of this layout: the rounded column means of the L.n points X (by
 // default L.Xs; the input rows give the same sums), computed once per call (L.shift).
-// nonfinite (optional, device): set to 1 if a value of X is NaN or infinite, else 0.
-const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X = nullptr, unsigned long long* nonfinite = nullptr);
+// screen (optional, two device words): [0] = 1 if a value of X is NaN or infinite, else 0;
+// [1] = the float bits of the largest |value|.
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X = nullptr, unsigned long long* screen = nullptr);
+// Whether the BF16 candidate test's squared terms stay in FP32's normal range for this
+// layout (its maxabs, d and radius); otherwise the FP32-direct tiles take the pairs.
+bool bf16_in_range(const Layout& L);
 // Ball centres (nb rows of L.d floats, radii rad; rows nb .. nb_pad - 1 padding) as BF16
 // rows of dp = 64 * ceil(d / 64) with {norm, a, q, radius or -1} per row (bf16_row).
 // Returns the mean relative widening of a ball pair's squared threshold by a and q.

@@ -868,9 +868,10 @@ __global__ void __launch_bounds__(32 * kRecheckWarps) k_recheck(const float* __r
 // Per-dimension column sums (double) of the real rows, d <= 256: a block step covers
 // 256 / d whole rows as one contiguous run of floats, so thread t always adds dimension
 // t % d; per-thread float partials, then one double atomic per dimension and block.
-// nonfinite (optional, zeroed by the caller): set to 1 if a value is NaN or infinite.
+// screen (optional, zeroed by the caller): screen[0] = 1 if a value is NaN or infinite,
+// screen[1] = the float bits of the largest |value| (NaNs aside).
 __global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, int64_t n, int d, double* __restrict__ sums,
-                                                unsigned long long* __restrict__ nonfinite)
+                                                unsigned long long* __restrict__ screen)
 {
     __shared__ float part[256];
     const int rpb = 256 / d;  // rows per step
@@ -878,16 +879,22 @@ __global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, in
     const bool active = t < rpb * d;
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
-    float acc = 0.f;
+    float acc = 0.f, mx = 0.f;
     bool bad = false;
     if (active)
         for (int64_t r = r0 + t / d; r < r1; r += rpb) {
             const float v = Xs[r * d + t % d];
             bad |= nonfinite_f32(v);
+            mx = fmaxf(mx, fabsf(v));
             acc += v;
         }
     part[t] = acc;
-    if (__syncthreads_or(bad) && nonfinite && t == 0) *nonfinite = 1ull;
+    if (screen) {
+        // non-negative floats order as their bit patterns
+        const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+        if ((t & 31) == 0 && m) atomicMax(&screen[1], (unsigned long long)m);
+    }
+    if (__syncthreads_or(bad) && screen && t == 0) screen[0] = 1ull;
     if (t < d) {
         double s2 = 0.0;
         for (int q = 0; q < rpb; ++q) s2 += (double)part[q * d + t];
@@ -1069,7 +1076,18 @@ double bf16_gamma(int d)
     return (double)dp * std::ldexp(1.0, -19) + (double)(d + 8) * std::ldexp(1.0, -24) + 2.0 * std::ldexp(1.0, -24);
 }
 
-const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X, unsigned long long* nonfinite)
+bool bf16_in_range(const Layout& L)
+{
+    // the centred rows lie within 2 max|x| + 1 (the shift is a rounded column mean): their
+    // squared norms, the Gram entries and the test's thresholds stay finite when
+    // d (2 max|x| + 1)^2 <= 2^124; a widened radius of at least 2^-40 keeps the underflow of
+    // products, norms and error radii (absolute errors of order d 2^-126) far below the
+    // test's relative slack kappa (eps_p)^2
+    const double m = 2.0 * (double)L.maxabs + 1.0;
+    return (double)L.d * m * m <= std::ldexp(1.0, 124) && widened_radius(L.radius, L.d) >= std::ldexp(1.f, -40);
+}
+
+const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X, unsigned long long* screen)
 {
     if (L.shift) return L.shift;
     if (!X) X = L.Xs;
@@ -1080,8 +1098,8 @@ const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X, unsigned long lo
     float* shift = (float*)(sums + d);
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 4));
-    if (nonfinite) RNNG_CUDA(cudaMemsetAsync(nonfinite, 0, sizeof(unsigned long long), s));
-    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums, nonfinite); ++c->launches;
+    if (screen) RNNG_CUDA(cudaMemsetAsync(screen, 0, 2 * sizeof(unsigned long long), s));
+    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums, screen); ++c->launches;
     k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
     L.shift = shift;
     return shift;

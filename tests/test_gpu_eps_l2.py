@@ -189,3 +189,22 @@ def test_unbounded_radius(ctx, orc, mode):
     wi, wv = orc.rips(60, u, v, w, 2)
     assert wi.size == 60 + 60 * 59 // 2 + 60 * 59 * 58 // 6
     assert np.array_equal(ids, wi) and np.array_equal(vals.view(np.uint32), wv.view(np.uint32))
+
+
+SCALES = [-75, -70, -60, -40, 40, 58, 61]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("e", SCALES)
+def test_power_of_two_scales(ctx, orc, mode, e):
+    """The same point set scaled by 2^e (exact in float32): RNNG's L2 of the scaled
+    points, subnormal squares at the small end included, decides the edges."""
+    rng = np.random.default_rng(88)
+    centres = rng.uniform(-4, 4, size=(6, 12))
+    base = (centres[rng.integers(0, 6, 2500)] + rng.normal(size=(2500, 12))).astype(np.float32)
+    s = np.float32(2.0 ** e)
+    x = (base * s).astype(np.float32)
+    r = np.float32(np.float32(2.6) * s)
+    want = orc.eps_graph_l2(x, r)
+    assert want[0].size > 3000
+    assert same(ctx.eps_graph_l2(x, r, mode=mode), want)

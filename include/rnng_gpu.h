@@ -178,7 +178,9 @@ int rnng_rips_edges(rnng_ctx* ctx, int64_t n, const int64_t* ids, const uint8_t*
 /* Graph finalisation: Graph(edges) + redistribute_edges at one rank
  * (include/graph.h:14, include/graph.hpp:59-116): from unordered edges, the list of
  * both orientations plus the self-loop (i, i, 0) of every vertex 0..num_vertices-1,
- * sorted by (u, v).  Output count = num_vertices + 2 * edges. */
+ * sorted by (u, v).  Output count = num_vertices + 2 * edges.  (RNNG's self-loops come
+ * from each point finding itself within the radius, so a point with a non-finite
+ * coordinate has none there; drop such rows' (i, i, 0) entries to match.) */
 int rnng_graph_finalize(rnng_ctx* ctx, const rnng_edges* edges, int64_t num_vertices, unsigned flags,
                         rnng_edges* out);
 

@@ -46,6 +46,30 @@ def test_oracle_rips_matches_reference(orc, name):
     assert int(dims.max()) == int(g["maxdim"])  # the top dimension is populated
 
 
+def test_reference_isolates_nan_rows():
+    """What RNNG's own paths did with NaN coordinates: the systolic and landmark drivers
+    give the same edges, no edge touches a row with a NaN, and the rips filtration keeps
+    those rows as vertices (value 0) with no higher simplex on them."""
+    a, b = golden("nan_systolic"), golden("nan_landmark")
+    for k in ("u", "v", "w"):
+        assert np.array_equal(a[k], b[k])
+    bad = np.nonzero(~np.isfinite(a["x"]).all(axis=1))[0]
+    assert bad.size == 45
+    assert not np.isin(a["u"], bad).any() and not np.isin(a["v"], bad).any()
+    r = golden("nan_rips")
+    bad_r = np.nonzero(~np.isfinite(r["x"]).all(axis=1))[0]
+    ids = np.asarray(r["ids"]).view(np.uint64)
+    dims = ids >> np.uint64(60)
+    verts = ids[dims == 0].astype(np.int64)
+    assert np.isin(bad_r, verts).all() and verts.size == int(r["n"])
+    # an edge id is a + C(b, 2) with a < b: no edge may carry a NaN row as either end
+    e = (ids[dims == 1] & np.uint64((1 << 60) - 1)).astype(np.int64)
+    hi = np.floor((1 + np.sqrt(1 + 8 * e.astype(np.float64))) / 2).astype(np.int64)
+    hi -= (hi * (hi - 1) // 2 > e)
+    lo = e - hi * (hi - 1) // 2
+    assert np.all(lo < hi) and not np.isin(hi, bad_r).any() and not np.isin(lo, bad_r).any()
+
+
 CELL_FIXTURES = ["k1_cells", "k1_cells_rips", "k3_cells", "dup_cells"]
 
 

@@ -189,20 +189,25 @@ int rnng_simplices_free(rnng_simplices* s);
 
 /* Allocation-free epsilon graph ------------------------------------------------------------
  * No counterpart in RNNG: an extra entry point for callers that cannot allocate device
- * memory when they need the graph (work issued during CUDA graph capture, inside another
- * library's stream callback, or in a process whose device allocator belongs to a
- * framework).  It takes no context and calls no cudaMalloc / cudaFree: the caller owns
- * every buffer, and the library's scratch is a fixed device array of about 12 MiB that
- * each GPU loading the library holds until exit.
+ * memory when they need the graph - a process whose device memory belongs to a
+ * framework's pool (a plugin gets buffers from it but may not call cudaMalloc beside
+ * it), a real-time loop that must not allocate after start-up, or a plugin host that
+ * forbids allocation inside the plugin.  It takes no context and calls no cudaMalloc /
+ * cudaFree: the caller owns every buffer, and the library's scratch is a fixed device
+ * array of about 12 MiB that each GPU loading the library holds until exit.
  *   X, ids (ids may be NULL = 0..n-1): device pointers; n <= 65536 points, d <= 4096;
  *   u, v, w: device arrays of `capacity` entries for the unordered edges u < v (any order);
  *   *count (host): number of edges found; stream: a cudaStream_t or NULL.
  * Same edges and bit-identical weights as rnng_eps_graph_l2 (all pairs are evaluated
- * with the reference's sequential FP32 L2).  Returns RNNG_ERR_INVALID beyond the size
- * limits and RNNG_ERR_OVERFLOW when more than min(capacity, 1048576) edges exist (the
- * first of them are written, *count holds the total).  The first call on a device looks
- * up the scratch address; make it before any stream capture.  Every call shares the one
- * scratch array, so calls whose GPU work overlaps race and must be serialised. */
+ * with the reference's sequential FP32 L2), the same RNNG_ERR_UNSUPPORTED for radius
+ * +inf with a row that holds an infinity and no NaN.  Returns RNNG_ERR_INVALID beyond
+ * the size limits and RNNG_ERR_OVERFLOW when more than min(capacity, 1048576) edges
+ * exist: then an unspecified subset of min(capacity, 1048576) of them is written (which
+ * ones can differ from call to call) and *count holds the total.  The call reads the
+ * count back to the host, so it synchronises `stream` before it returns.  The first
+ * call on a device looks up the scratch address; make it before any stream capture.
+ * Every call shares the one scratch array, so calls whose GPU work overlaps race and
+ * must be serialised. */
 int rnng_eps_graph_l2_static(const float* X, const int64_t* ids, int64_t n, int64_t d, float radius, int64_t* u,
                              int64_t* v, float* w, int64_t capacity, int64_t* count, void* stream);
 

@@ -1,25 +1,30 @@
 // Allocation-free epsilon graph: rnng_eps_graph_l2_static (include/rnng_gpu.h).
 //
 // Some callers cannot allocate device memory at the point where they need the graph:
-// code that runs while a CUDA graph is being captured, inside another library's
-// stream callback or memory pool, or in a process whose allocator is owned by a
-// framework.  For them this entry point takes only caller-owned device buffers
+// a process whose device memory is owned by a framework's pool (the framework hands
+// out buffers but a plugin may not call cudaMalloc beside it), a real-time loop that
+// must not allocate after start-up, or a plugin host that forbids allocation inside
+// the plugin.  For them this entry point takes only caller-owned device buffers
 // (points in, edges out) and keeps its own scratch in a fixed, file-scope device
 // array, so it never calls cudaMalloc, cudaFree or any allocating library routine.
 //
-// Scratch: an edge counter and up to kStaticEdges staged edges (two 32-bit point
-// indices and the distance, 12 bytes each) - about 12 MiB that every GPU which loads
-// the library keeps until the process exits.  Points are evaluated all pairs by all
-// pairs in 128 x 128 tiles with RNNG's sequential FP32 L2 (no partition, so no further
-// scratch), which bounds the problem size: n <= kStaticMaxPoints, d <= kStaticMaxDim.
+// Scratch: an edge counter, a flag word and up to kStaticEdges staged edges (two 32-bit
+// point indices and the distance, 12 bytes each) - about 12 MiB that every GPU which
+// loads the library keeps until the process exits.  Points are evaluated all pairs by
+// all pairs in 128 x 128 tiles with RNNG's sequential FP32 L2 (no partition, so no
+// further scratch), which bounds the problem size: n <= kStaticMaxPoints,
+// d <= kStaticMaxDim.
 //
 // The device address of the array is looked up with cudaGetSymbolAddress once per
 // device, on the first call made with that device current; make that first call
 // before any stream capture.  All calls share the one array and it keeps the last
-// call's contents; the counter is cleared at the start of every call.  Calls whose
-// GPU work overlaps (different streams, or different host threads on one device)
-// race on the array and must be serialised by the caller.
+// call's contents; the counter and the flag are cleared at the start of every call.
+// Calls whose GPU work overlaps (different streams, or different host threads on one
+// device) race on the array and must be serialised by the caller.  Every call reads
+// the edge count back to the host, so it synchronises the caller's stream before it
+// returns.
 #include <cuda_runtime.h>
+#include <math.h>
 
 #include <mutex>
 
@@ -35,7 +40,8 @@ constexpr int kMaxDevices = 64;
 
 struct __align__(256) Scratch {
     unsigned long long count;
-    unsigned long long pad[31];
+    unsigned long long flag;  // 1: a row holds an infinity and no NaN (set only at radius +inf)
+    unsigned long long pad[30];
     uint32_t si[kStaticEdges];
     uint32_t sj[kStaticEdges];
     float w[kStaticEdges];
@@ -144,6 +150,27 @@ __global__ void __launch_bounds__(256) k_static_tiles(const float* __restrict__ 
     }
 }
 
+// Radius +inf only: raises sc->flag when some row holds an infinite coordinate and no
+// NaN.  Such a row is at L2 +inf (not NaN) from the finite rows, so `+inf <= +inf`
+// would make those pairs edges; the regular entry point refuses that case, and so does
+// this one.  One warp per row.
+__global__ void k_static_screen(const float* __restrict__ X, int64_t n, int d, Scratch* __restrict__ sc)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += warps) {
+        bool has_inf = false, has_nan = false;
+        for (int k = lane; k < d; k += 32) {
+            const float x = X[r * d + k];
+            has_inf |= isinf(x);
+            has_nan |= isnan(x);
+        }
+        has_inf = __any_sync(0xffffffffu, has_inf);
+        has_nan = __any_sync(0xffffffffu, has_nan);
+        if (lane == 0 && has_inf && !has_nan) atomicExch(&sc->flag, 1ull);
+    }
+}
+
 // Staged edges -> the caller's arrays in id space with u < v.
 __global__ void k_static_out(const Scratch* __restrict__ sc, int64_t m, const int64_t* __restrict__ ids,
                              int64_t* __restrict__ u, int64_t* __restrict__ v, float* __restrict__ w)
@@ -193,22 +220,33 @@ extern "C" int rnng_eps_graph_l2_static(const float* X, const int64_t* ids, int6
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Scratch* sc = nullptr;
     if (scratch_for_current_device(&sc) != cudaSuccess) return RNNG_ERR_CUDA;
-    // the counter starts at zero on every call (the array keeps the previous call's contents)
-    if (cudaMemsetAsync(&sc->count, 0, sizeof(unsigned long long), s) != cudaSuccess) return RNNG_ERR_CUDA;
+    // the counter and the flag start at zero on every call (the array keeps the previous
+    // call's contents)
+    if (cudaMemsetAsync(&sc->count, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess) return RNNG_ERR_CUDA;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return RNNG_ERR_CUDA;
+    if (n >= 2 && radius == INFINITY) {
+        const int64_t blocks = (n + 7) / 8;
+        k_static_screen<<<(int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8), 256, 0, s>>>(X, n, (int)d,
+                                                                                                  sc);
+        if (cudaGetLastError() != cudaSuccess) return RNNG_ERR_CUDA;
+    }
     if (n >= 2 && radius >= 0.f) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int64_t T = (n + kTileS - 1) / kTileS;
         const int64_t pairs = T * (T + 1) / 2;
         const int grid = (int)(pairs < (int64_t)sms * 4 ? pairs : (int64_t)sms * 4);
         k_static_tiles<<<grid, 256, 0, s>>>(X, n, (int)d, radius, sc);
         if (cudaGetLastError() != cudaSuccess) return RNNG_ERR_CUDA;
     }
-    unsigned long long found = 0;
-    if (cudaMemcpyAsync(&found, &sc->count, sizeof(found), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    // the count and the flag, read back together
+    unsigned long long head[2] = {0ull, 0ull};
+    if (cudaMemcpyAsync(head, &sc->count, sizeof(head), cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return RNNG_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return RNNG_ERR_CUDA;
+    if (head[1]) return RNNG_ERR_UNSUPPORTED;  // radius +inf with an infinite, NaN-free row
+    const unsigned long long found = head[0];
     *count = (int64_t)found;
     const int64_t staged = (int64_t)found < kStaticEdges ? (int64_t)found : kStaticEdges;
     const int64_t m = staged < capacity ? staged : capacity;

@@ -26,6 +26,13 @@ def build(ref: bool = False) -> None:
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 
+def ref_source_dir() -> str | None:
+    """The RNNG source tree the recipe builds from ($RNNG_SRC, see oracle/Makefile), if present."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref-src"], capture_output=True, text=True)
+    out = r.stdout.strip()
+    return out if r.returncode == 0 and out else None
+
+
 def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
@@ -60,6 +67,11 @@ def lib() -> ctypes.CDLL:
         L.orc_dist_matrix_l2.argtypes = [_f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int64, _f32p]
         L.orc_dist_matrix_edit.argtypes = [ctypes.c_void_p, _i64p, ctypes.c_int64, ctypes.c_void_p, _i64p,
                                            ctypes.c_int64, _f32p]
+        L.orc_landmark_l2.restype = ctypes.c_int64
+        L.orc_landmark_l2.argtypes = [_f32p, ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_int64,
+                                      ctypes.c_float, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_i64p),
+                                      ctypes.POINTER(_i64p), ctypes.POINTER(_f32p),
+                                      ctypes.POINTER(ctypes.c_double), _i64p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -113,6 +125,26 @@ def eps_graph_l2(X: np.ndarray, eps, rows: tuple[int, int] | None = None):
     cnt = lib().orc_eps_graph_l2(X.ctypes.data_as(_f32p), n, d, ctypes.c_float(eps), r0, r1,
                                  ctypes.byref(pu), ctypes.byref(pv), ctypes.byref(pw))
     return _edges(cnt, pu, pv, pw)
+
+
+LANDMARK_PHASES = ("voronoi", "cells", "ghosts", "neighbours", "graph")
+
+
+def landmark_l2(X: np.ndarray, eps, num_centers: int, cover: float = 1.5, leaf_size: int = 10, seed: int = 7):
+    """RNNG's landmark pipeline (Voronoi cells, cover trees, ghosts, batched radius
+    queries; oracle/landmark.c) on the host threads: (u, v, w) sorted, and a dict of
+    phase seconds and counts."""
+    X = np.ascontiguousarray(X, np.float32)
+    n, d = X.shape
+    pu, pv, pw = _i64p(), _i64p(), _f32p()
+    ph = (ctypes.c_double * 5)()
+    st = (ctypes.c_int64 * 3)()
+    cnt = lib().orc_landmark_l2(X.ctypes.data_as(_f32p), n, d, ctypes.c_float(eps), num_centers,
+                                ctypes.c_float(cover), leaf_size, seed, ctypes.byref(pu), ctypes.byref(pv),
+                                ctypes.byref(pw), ph, st)
+    info = {k: ph[i] for i, k in enumerate(LANDMARK_PHASES)}
+    info.update({"seconds": sum(ph), "num_cells": int(st[0]), "num_ghosts": int(st[1]), "threads": int(st[2])})
+    return _edges(cnt, pu, pv, pw, sort=False), info
 
 
 def cross_l2(X: np.ndarray, Q: np.ndarray, eps):

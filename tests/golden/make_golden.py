@@ -6,7 +6,7 @@ source tree with the single-rank MPI shim (oracle/Makefile, target ``ref``), thr
 the binary-dump harness oracle/ref_harness.cpp, which makes the same API calls as
 RNNG's drivers.  The expected outputs are stored with full float bits.
 
-    make -C oracle ref            # needs the RNNG sources (REF=/path/to/RNNG)
+    make -C oracle ref            # needs the RNNG sources (RNNG_SRC=/path/to/RNNG)
     python tests/golden/make_golden.py [fixture names]   # default: all of them
 
 Fixtures (npz, inputs + expected):

@@ -9,6 +9,11 @@ import pytest
 from conftest import ROOT
 
 
+def _have_rnng_sources() -> bool:
+    import oracle
+    return oracle.ref_source_dir() is not None
+
+
 def declared():
     text = open(os.path.join(ROOT, "include", "rnng_gpu.h")).read()
     return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(rnng_\w+)\s*\(", text, re.M)))
@@ -44,7 +49,7 @@ def test_dropin_harness_builds_against_the_dropin_headers():
     assert os.path.exists(os.path.join(ROOT, "oracle", "_build", "dropin_harness"))
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/drivers"), reason="needs the RNNG driver sources")
+@pytest.mark.skipif(not _have_rnng_sources(), reason="needs the RNNG sources ($RNNG_SRC) to build its drivers")
 def test_unchanged_reference_drivers_build_against_the_dropin_headers():
     """drivers/systolic.cpp, landmark.cpp and rips.cpp, unmodified, compile against the
     drop-in headers and link to librnng_gpu.so and the single-rank MPI shim."""

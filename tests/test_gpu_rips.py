@@ -185,7 +185,7 @@ def test_torus_100k_against_oracle_cliques(ctx, orc):
     from rnng_gb300 import synth
     x = synth.torus16(n=100_000, seed=4)
     r = synth.choose_eps(x, 30.0, sample=20000)
-    u, v, w = ctx.eps_graph_l2(x, r, mode="fp32")
+    u, v, w = orc.eps_graph_l2(x, r)  # the oracle's own edges, all pairs
     want = orc.rips(x.shape[0], u, v, w, 2)
     got = ctx.rips_l2(x, r, maxdim=2, mode="bf16")
     assert same(got, want) and got[0].size > 1_000_000

@@ -9,6 +9,12 @@ import pytest
 
 from conftest import ROOT, golden, golden_points
 
+
+def _have_rnng_sources() -> bool:
+    import oracle
+    return oracle.ref_source_dir() is not None
+
+
 EDGE_FIXTURES = ["k1_systolic", "k1_landmark", "k2_landmark", "k5_landmark", "nan_systolic", "nan_landmark"]
 
 
@@ -161,7 +167,7 @@ def test_rips_against_brute_force(orc):
     assert np.array_equal(vals, np.array([val for val, _ in want], np.float32))
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="needs the RNNG sources to build its drivers")
+@pytest.mark.skipif(not _have_rnng_sources(), reason="needs the RNNG sources ($RNNG_SRC) to build its drivers")
 def test_unchanged_reference_drivers_agree(orc, tmp_path):
     """RNNG's own drivers, built unchanged against the MPI shim, report the fixture's counts."""
     orc.build(ref=True)

@@ -9,8 +9,9 @@ is timed beside it, and both produce the identical edge set.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-With --impl reference the CPU restatement of RNNG's path is timed on the host cores
-(see cpu_leg below) on a bounded sample of the same workload.  Under torchrun (N > 1)
+With --impl reference RNNG's own algorithm for the path (its landmark pipeline,
+restated in C under oracle/) is timed on the host cores on a prefix sample of the same
+workload (see cpu_landmark_leg below).  Under torchrun (N > 1)
 every rank runs an independent replica on its own GPU (the path is not sharded).
 Prints one JSON line on rank 0.
 """
@@ -110,8 +111,44 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- CPU leg
 
+LANDMARK_PREFIX = 100_000  # points of the CPU reference sample
+POINTS_PER_CELL = 1_000    # RNNG's landmark run of the descriptor workload: 1,000 landmarks for 1M points
+
+
+def cpu_landmark_leg(x, radius, prefix: int = LANDMARK_PREFIX, centres: int | None = None,
+                     threads: int | None = None) -> dict:
+    """Times RNNG's own algorithm on the host cores: its landmark pipeline (Voronoi cells,
+    cover trees, ghost points, batched radius queries; restated in oracle/landmark.c and
+    checked there against RNNG's driver) over the first `prefix` points, with one landmark
+    per POINTS_PER_CELL points as RNNG's run of this workload uses.  Edges/s of the sample:
+    RNNG's cost per edge grows with n (the Voronoi step alone is n x landmarks), so the
+    sample's rate is an upper bound of its full-size rate."""
+    import oracle
+    oracle.build()
+    full = oracle.num_threads()
+    if threads:
+        oracle.set_threads(threads)
+    xs = np.ascontiguousarray(x[:prefix])
+    m = centres or max(1, xs.shape[0] // POINTS_PER_CELL)
+    t0 = time.perf_counter()
+    (u, v, w), info = oracle.landmark_l2(xs, radius, num_centers=m)
+    dt = time.perf_counter() - t0
+    if threads:
+        oracle.set_threads(full)
+    return {"value": u.size / dt, "edges": int(u.size), "seconds": dt, "points": int(xs.shape[0]),
+            "landmarks": m, "threads": info["threads"], "host_cores": os.cpu_count(),
+            "phases_s": {k: round(info[k], 3) for k in oracle.LANDMARK_PHASES}}
+
+
+def landmark_sample_text(leg: dict) -> str:
+    return (f"RNNG's landmark pipeline (oracle/landmark.c) on the first {leg['points']} points, "
+            f"{leg['landmarks']} landmarks, {leg['threads']} host threads of {leg['host_cores']} cores: "
+            f"{leg['edges']} edges in {leg['seconds']:.2f} s")
+
+
 def cpu_leg(x, radius, budget_s: float = 20.0, threads: int | None = None) -> dict:
-    """Times the CPU restatement of RNNG's path on a bounded sample of the workload.
+    """Times the brute-force restatement on a bounded sample of the workload (a second,
+    labelled CPU number beside RNNG's algorithm).
 
     The oracle evaluates the reference predicate (sequential FP32 L2 <= radius) for a
     strided sample of query rows against all points; the measured time per pair
@@ -302,13 +339,17 @@ def main():
                 "flops_per_launch": 2.0 * d * pairs, "ms_per_launch": g_ms,
                 "algorithmic": "2*d flops per evaluated point pair (x.y), pairs = surviving tile pairs * 128 * 128"}
 
-    # ---- CPU baseline (rank 0 only)
-    cpu = None
+    # ---- CPU baselines (rank 0 only): RNNG's algorithm on a prefix, and brute force
+    cpu, brute = None, None
     if rank == 0 and not args.no_cpu:
-        leg = cpu_leg(x, radius)
-        cpu = {"value": cpu_value(leg, edges, n), "unit": UNIT, "cores": leg["cores"], "kind": "port",
-               "sample": f"{leg['rows']} strided query rows x all {n} points with the oracle's reference "
-                         f"predicate ({leg['seconds']:.1f} s), time per pair scaled to n(n-1)/2 pairs"}
+        leg = cpu_landmark_leg(x, radius)
+        cpu = {"value": leg["value"], "unit": UNIT, "cores": leg["threads"], "kind": "port",
+               "algorithm": "RNNG landmark pipeline (Voronoi cells + cover trees + ghosts)",
+               "sample": landmark_sample_text(leg), "phases_s": leg["phases_s"]}
+        bl = cpu_leg(x, radius, budget_s=8.0)
+        brute = {"value": cpu_value(bl, edges, n), "unit": UNIT, "cores": bl["cores"],
+                 "sample": f"{bl['rows']} strided query rows x all {n} points with the oracle's reference "
+                           f"predicate ({bl['seconds']:.1f} s), time per pair scaled to n(n-1)/2 pairs"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -324,6 +365,7 @@ def main():
                                                ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles", "ms_recheck",
                                                 "ms_finalize")}}, n),
                 "fp32_direct": fp32, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "cpu_bruteforce": brute,
                 "max_abs_err_fp64": err64, "gpu_launches": int(sum(launches)), "clocks": clk}
         print(json.dumps(line), flush=True)
     if dist:
@@ -447,6 +489,17 @@ def run_secondary(args, world, rank, local):
     err64 = None
     if rank == 0:
         err64 = 0.0 if err_edges is None else fp64_error(x, *err_edges())
+    cpu = None
+    if rank == 0 and not args.no_cpu and wl in ("k1", "k5"):
+        # k1: RNNG's systolic run is one cover tree over all points (one cell); k5: a prefix
+        # with RNNG's 1,024 landmarks per 5M points
+        leg = (cpu_landmark_leg(x, radius, prefix=n, centres=1) if wl == "k1"
+               else cpu_landmark_leg(x, radius, prefix=LANDMARK_PREFIX,
+                                     centres=max(1, LANDMARK_PREFIX * 1024 // 5_000_000)))
+        cpu = {"value": leg["value"], "unit": SECONDARY[wl]["unit"], "cores": leg["threads"], "kind": "port",
+               "algorithm": "RNNG cover-tree search" + (" (one cell: systolic)" if wl == "k1" else
+                                                        " with landmark cells and ghosts"),
+               "sample": landmark_sample_text(leg), "phases_s": leg["phases_s"]}
     roofline = None
     if wl == "k3" and last["ms_gram"] > 0:
         # the filter: a Gram form over 512-byte E4M3 rows (thermometer-coded q-gram profiles)
@@ -485,7 +538,7 @@ def run_secondary(args, world, rank, local):
                 "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)", "config": cfg, "fp32_direct": fp32,
                 "e2e": {"value": world * units / e2e_s, "unit": SECONDARY[wl]["unit"], "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(units * d2h_per_unit), "ms_per_step": e2e_s * 1e3},
-                "roofline": roofline, "cpu_baseline": None, "max_abs_err_fp64": err64,
+                "roofline": roofline, "cpu_baseline": cpu, "max_abs_err_fp64": err64,
                 "gpu_launches": int(sum(launches)), "clocks": clk}
         print(json.dumps(line), flush=True)
     if dist:
@@ -506,26 +559,32 @@ def read_profile_traffic():
 
 
 def run_reference(args, world, rank):
-    """Reference arm: RNNG's CPU path restated by the oracle, timed on the host cores."""
+    """Reference arm: RNNG's own algorithm for this path (its landmark pipeline, restated
+    in oracle/landmark.c) on all host cores, each step one run over a prefix sample of
+    the same workload (RNNG's C++ cannot be built on the GPU machine: its sources are not
+    there)."""
     if rank != 0:
+        return
+    if args.workload != "k2":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the headline (k2) only"}))
         return
     x, radius = workload(args.points)
     n = x.shape[0]
-    vals = []
+    vals, leg = [], None
     for i in range(args.warmup + args.steps):
-        leg = cpu_leg(x, radius, budget_s=10.0)
-        # edges of the whole job estimated from the sampled rows' mean degree
-        edges = n * leg["mean_degree"] / 2
+        leg = cpu_landmark_leg(x, radius)
         if i >= args.warmup:
-            vals.append(cpu_value(leg, edges, n))
+            vals.append(leg["value"])
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": leg["seconds"] * 1e3,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
             "config": config(n=n), "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": leg["cores"], "kind": "port",
-                             "sample": f"{leg['rows']} strided query rows x all {n} points per step"}}
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": leg["threads"], "kind": "port",
+                             "algorithm": "RNNG landmark pipeline (Voronoi cells + cover trees + ghosts)",
+                             "sample": landmark_sample_text(leg) + " per step"}}
     print(json.dumps(line), flush=True)
 
 

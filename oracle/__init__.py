@@ -138,12 +138,13 @@ def landmark_l2(X: np.ndarray, eps, num_centers: int, cover: float = 1.5, leaf_s
     n, d = X.shape
     pu, pv, pw = _i64p(), _i64p(), _f32p()
     ph = (ctypes.c_double * 5)()
-    st = (ctypes.c_int64 * 3)()
+    st = (ctypes.c_int64 * 4)()
     cnt = lib().orc_landmark_l2(X.ctypes.data_as(_f32p), n, d, ctypes.c_float(eps), num_centers,
                                 ctypes.c_float(cover), leaf_size, seed, ctypes.byref(pu), ctypes.byref(pv),
                                 ctypes.byref(pw), ph, st)
     info = {k: ph[i] for i, k in enumerate(LANDMARK_PHASES)}
-    info.update({"seconds": sum(ph), "num_cells": int(st[0]), "num_ghosts": int(st[1]), "threads": int(st[2])})
+    info.update({"seconds": sum(ph), "num_cells": int(st[0]), "num_ghosts": int(st[1]), "threads": int(st[2]),
+                 "empty_cells": int(st[3])})
     return _edges(cnt, pu, pv, pw, sort=False), info
 
 

@@ -182,3 +182,37 @@ def test_unchanged_reference_drivers_agree(orc, tmp_path):
         assert f"edges={int(g['reported_edges'])}" in r.stderr
         lines = open(out).read().split("\n")
         assert lines[0].split()[-1] == str(int(g["reported_edges"]))
+
+
+@pytest.mark.parametrize("name,centres", [("k1_systolic", 30), ("k2_landmark", 12), ("k5_landmark", 25),
+                                          ("nan_landmark", 9)])
+def test_landmark_pipeline_port_matches_brute_force(orc, name, centres):
+    """RNNG's landmark pipeline restated on the CPU (oracle/landmark.c: Voronoi cells,
+    cover trees, ghosts, batched radius queries) finds exactly the brute-force edges,
+    on one thread and on all threads."""
+    g = golden(name)
+    x = golden_points(g)
+    want = orc.eps_graph_l2(x, g["radius"])
+    full = orc.num_threads()
+    for threads in (1, full):
+        orc.set_threads(threads)
+        (u, v, w), info = orc.landmark_l2(x, g["radius"], num_centers=centres)
+        assert np.array_equal(u, want[0]) and np.array_equal(v, want[1])
+        assert np.array_equal(w.view(np.uint32), want[2].view(np.uint32))
+        assert info["num_cells"] == centres and info["threads"] == threads
+    orc.set_threads(full)
+
+
+def test_landmark_pipeline_port_duplicates_and_tiny(orc):
+    rng = np.random.default_rng(5)
+    x = np.repeat(rng.normal(size=(40, 5)).astype(np.float32), 7, axis=0)
+    for r, m in ((0.0, 10), (0.8, 40), (5.0, 3), (0.8, 25)):
+        want = orc.eps_graph_l2(x, np.float32(r))
+        (u, v, w), info = orc.landmark_l2(x, np.float32(r), num_centers=m)
+        if info["empty_cells"] == 0:
+            assert np.array_equal(u, want[0]) and np.array_equal(v, want[1])
+        else:  # RNNG's ghost step indexes cells by non-empty position: edges can go missing
+            assert np.isin(u * x.shape[0] + v, want[0] * x.shape[0] + want[1]).all()
+    for n in (0, 1, 2):
+        (u, v, w), _ = orc.landmark_l2(np.zeros((n, 3), np.float32), 1.0, num_centers=1)
+        assert u.size == (1 if n == 2 else 0)

@@ -356,14 +356,16 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
                 "config": config({"parallelism": "replicas" if world > 1 else "single-gpu",
-                                  "edges": int(edges), "tile_pairs": int(last["tile_pairs"]),
+                                  "edges": int(edges), "super_pairs": int(last["super_pairs"]),
+                                  "tile_pairs": int(last["tile_pairs"]),
                                   "tile_pairs_all": int(last["tile_pairs_all"]),
                                   "candidates": int(last["candidates"]),
                                   "prune": {"tensor_cores": bool(last["prune_tensor"]),
                                             "widen": round(float(last["prune_widen"]), 4)},
                                   "stage_ms": {k: round(last[k], 3) for k in
                                                ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles", "ms_recheck",
-                                                "ms_finalize")}}, n),
+                                                "ms_finalize")},
+                                  "gram": {k: int(last[k]) for k in ("gram_nt", "gram_chunk", "gram_slots")}}, n),
                 "fp32_direct": fp32, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "cpu_bruteforce": brute,
                 "max_abs_err_fp64": err64, "gpu_launches": int(sum(launches)), "clocks": clk}
@@ -530,7 +532,8 @@ def run_secondary(args, world, rank, local):
         cfg.update({"units": int(units), "parallelism": "replicas" if world > 1 else "single-gpu",
                     "stage_ms": {k: round(last[k], 3) for k in ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles",
                                                                 "ms_recheck", "ms_finalize", "ms_total")},
-                    "tile_pairs": int(last["tile_pairs"]), "candidates": int(last["candidates"]),
+                    "super_pairs": int(last["super_pairs"]), "tile_pairs": int(last["tile_pairs"]),
+                    "candidates": int(last["candidates"]),
                     "prune": {"tensor_cores": bool(last["prune_tensor"]), "widen": round(float(last["prune_widen"]), 4)}})
         line = {"metric": SECONDARY[wl]["metric"], "value": value, "unit": SECONDARY[wl]["unit"], "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

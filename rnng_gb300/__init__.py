@@ -35,6 +35,7 @@ MODES = {"fp32": 0, "bf16": 1}
 # every entry point include/rnng_gpu.h declares
 EXPORTS = [
     "rnng_ctx_create", "rnng_ctx_destroy", "rnng_last_error", "rnng_get_stats", "rnng_ctx_stream", "rnng_ctx_trim",
+    "rnng_ctx_set_gram_tuning",
     "rnng_eps_graph_l2", "rnng_radius_query_l2", "rnng_voronoi_l2", "rnng_eps_graph_edit", "rnng_rips_l2",
     "rnng_graph_finalize", "rnng_edges_free", "rnng_simplices_free", "rnng_eps_graph_l2_static",
     "rnng_voronoi_edit", "rnng_rips_edges",
@@ -62,7 +63,8 @@ class Stats(ctypes.Structure):
                                                  "ms_prune", "ms_tiles", "ms_recheck", "ms_finalize", "ms_d2h")] + \
                [(k, ctypes.c_int64) for k in ("num_cells", "super_pairs", "tile_pairs", "tile_pairs_all", "pairs_evaluated",
                                               "candidates", "edges", "retries", "simplices", "kernel_launches")] + \
-               [("ms_gram", ctypes.c_double), ("prune_widen", ctypes.c_double), ("prune_tensor", ctypes.c_int64)]
+               [("ms_gram", ctypes.c_double), ("prune_widen", ctypes.c_double), ("prune_tensor", ctypes.c_int64),
+                ("gram_nt", ctypes.c_int64), ("gram_chunk", ctypes.c_int64), ("gram_slots", ctypes.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,6 +91,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rnng_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     L.rnng_ctx_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.rnng_ctx_trim.argtypes = [vp]
+    L.rnng_ctx_set_gram_tuning.argtypes = [vp, ip, ip, ip]
     L.rnng_eps_graph_l2.argtypes = [vp, vp, vp, i64, i64, f32, ip, u32, ctypes.POINTER(Edges)]
     L.rnng_radius_query_l2.argtypes = [vp, vp, vp, i64, vp, vp, i64, i64, f32, u32, ctypes.POINTER(Edges)]
     L.rnng_voronoi_l2.argtypes = [vp, vp, i64, vp, i64, i64, u32, vp, vp]
@@ -170,6 +173,11 @@ class Context:
         s = Stats()
         self._check(self.lib.rnng_get_stats(self.h, ctypes.byref(s)), self.h)
         return s.as_dict()
+
+    def set_gram_tuning(self, nt: int = 0, chunk: int = 0, slots: int = 0) -> None:
+        """Forces the Gram kernel's column tiles per item, queue chunk and B slots (0: the
+        tuning table's value or the default)."""
+        self._check(self.lib.rnng_ctx_set_gram_tuning(self.h, nt, chunk, slots), self.h)
 
     def stream(self) -> int:
         p = ctypes.c_void_p()

@@ -115,9 +115,16 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
     // the BF16 candidate test needs its squared terms in FP32's normal range (coordinates
     // up to about 2^61 / sqrt(d), a radius of at least 2^-40); beyond it the FP32-direct
     // tiles evaluate the surviving tile pairs
-    const int tmode = (mode == RNNG_MODE_BF16_RECHECK && !bf16_in_range(L)) ? RNNG_MODE_FP32_DIRECT : mode;
+    // tiles of few dimensions (d < kBf16MinDim, padded to 64 for the tensor cores) are
+    // faster on the CUDA cores: at d = 8 (20k points) the FP32-direct tiles took 1.05 ms per
+    // call against 1.25 ms for the BF16 Gram form, at d = 16 the Gram form was 1.2x faster
+    const bool bf16_tiles = bf16_in_range(L) && L.d >= kBf16MinDim;
+    const int tmode = (mode == RNNG_MODE_BF16_RECHECK && !bf16_tiles) ? RNNG_MODE_FP32_DIRECT : mode;
     if (tmode == RNNG_MODE_BF16_RECHECK) {
-        schedule_items(c, L, c->num_sms, gram_item_tiles(L.d));
+        const GramTune t = gram_tune(c, 0, (int)ceil_div(L.d, 64) * 64, (int64_t)L.tile_pairs);
+        L.gram_chunk = t.chunk;
+        L.gram_slots = t.slots;
+        schedule_items(c, L, t.nt);
         prepare_bf16(c, L);
     }
     const int64_t m = tiles_with_retry(c, L, tmode, E);
@@ -151,6 +158,7 @@ int rnng_ctx_create(int device, rnng_ctx** out)
         c->own_stream = true;
         ensure_events(c);
         init_device_fault(c);
+        load_gram_table(c);
     });
     if (rc != RNNG_OK) {
         delete c;
@@ -187,6 +195,15 @@ int rnng_ctx_stream(rnng_ctx* c, void** stream)
 {
     if (!c || !stream) return RNNG_ERR_INVALID;
     *stream = (void*)c->stream;
+    return RNNG_OK;
+}
+
+int rnng_ctx_set_gram_tuning(rnng_ctx* c, int nt, int chunk, int slots)
+{
+    if (!c || nt < 0 || nt > 2 || chunk < 0 || slots < 0 || slots == 1) return RNNG_ERR_INVALID;
+    c->gram_force.nt = nt;
+    c->gram_force.chunk = chunk;
+    c->gram_force.slots = slots;
     return RNNG_OK;
 }
 

@@ -1,11 +1,14 @@
 // Tile covers and exact tile-pair pruning by the triangle inequality.
 //
 // Every tile (128 consecutive points of the partition order) is covered by up to
-// kBalls balls: the tile is split by farthest-point bisection (take the group with
-// the largest radius, its point a farthest from the centroid, the point b farthest
-// from a, and move the points closer to b than to a into a new group) until it has
-// kBalls groups; each group is stored as (centroid, radius).  A super-tile (kSuper
-// consecutive tiles) gets kBalls balls built the same way from its tiles' balls.
+// kTileBalls balls: greedy k-center groups (the first centre farthest from the tile's
+// centroid, each next one the point farthest from the chosen centres, every point in the
+// group of its nearest centre), each group stored as (centroid, radius).  A super-tile
+// (kSuper consecutive tiles) gets kSuperBalls balls built the same way from its tiles'
+// balls.  The greedy gives every separate cluster, and every stray point of another
+// cluster, its own ball before it splits a cluster, so a tile that the partition mixed
+// from several clusters still gets tight balls (farthest-point bisection into four balls
+// left 5.2M of the 30.5M tile pairs of the 1M x 128 descriptors; these covers far fewer).
 // A pair of tiles (or super-tiles) is skipped when every pair of their balls is
 // separated:  |c1 - c2| (1 - relerr) > eps' + r1 + r2, with radii widened by the
 // relative error of their float computation and eps' = eps * (1 + (d+8) 2^-24).
@@ -100,237 +103,170 @@ __global__ void __launch_bounds__(256) k_chain_leaves(const float* __restrict__ 
 }
 
 // ------------------------------------------------------------------------------------------------
-// farthest-point bisection shared by tile balls (over points) and super balls (over balls)
+// covers: farthest-point (k-center) groups, shared by tile balls (over points) and super
+// balls (over tile balls)
+//
+// Items are rows of `src` (points, or ball centres with item radii `irad`); one thread
+// per item (at most kCoverItems items).  The first centre is the item farthest from the
+// items' centroid; each further centre is the item farthest from all chosen centres
+// (Gonzalez' greedy k-center), every item joins its nearest centre, and the greedy stops
+// early once every item coincides with a centre.  In clustered data the greedy takes a
+// centre in every separate cluster (and every stray point) before it splits a cluster,
+// so the groups follow the clusters.  Each group is then stored as (centroid, radius),
+// the radius measured from the centroid, so the ball covers its members; radii are
+// widened by the relative error of their float computation (`grow`).
 
-// Per-block workspace.  Items are rows of `src` (points, or ball centres with
-// item radii `irad`).  Dimensions are walked with a stride so d is unbounded.
-struct BisectState {
-    int label[kSuper * kBalls > kTile ? kSuper * kBalls : kTile];
-    float dist[kSuper * kBalls > kTile ? kSuper * kBalls : kTile];
-    float rad[kBalls];
-    int far_idx[kBalls];
-    int count[kBalls];
-    int ngroups;
-    int a, b;
-    float red_v[65];
-    int red_i[66];
-    float part[256];  // centroid partial sums (blockDim <= 256)
-    int pcnt[256];
+constexpr int kCoverItems = kTile > kSuper * kTileBalls ? kTile : kSuper * kTileBalls;
+constexpr int kCoverMaxBalls = kTileBalls > kSuperBalls ? kTileBalls : kSuperBalls;
+constexpr int kCoverThreads = kCoverItems;
+
+struct CoverState {
+    int label[kCoverItems];
+    unsigned rad_bits[kCoverMaxBalls];  // group radius (non-negative float bits, atomicMax)
+    int count[kCoverMaxBalls];
+    float red_v[kCoverThreads / 32];
+    int red_i[kCoverThreads / 32];
+    int pick;
+    float pick_v;
 };
 
-// (max value, index) of a pair (ties -> smaller index), and a count summed alongside
-__device__ __forceinline__ void argmax_step(float& v, int& i, int& n, float ov, int oi, int on)
+// distance of item r (row x, d floats) to row v, sequential fmaf over the dimensions
+__device__ __forceinline__ float row_dist(const float* __restrict__ x, const float* __restrict__ v, int d)
 {
-    if (ov > v || (ov == v && oi < i)) {
-        v = ov;
-        i = oi;
-    }
-    n += on;
-}
-
-// block-wide (max value, index) reduction with ties -> smaller index, plus the sum of
-// `cnt`: warp shuffles, then one warp over the per-warp results (two block barriers)
-__device__ void block_argmax(BisectState& st, float v, int i, float& out_v, int& out_i, int cnt, int* out_cnt)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        argmax_step(v, i, cnt, __shfl_xor_sync(0xffffffffu, v, o), __shfl_xor_sync(0xffffffffu, i, o),
-                    __shfl_xor_sync(0xffffffffu, cnt, o));
-    if (lane == 0) {
-        st.red_v[warp] = v;
-        st.red_i[warp] = i;
-        st.red_i[32 + warp] = cnt;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        float wv = lane < nw ? st.red_v[lane] : -INFINITY;
-        int wi = lane < nw ? st.red_i[lane] : -1;
-        int wn = lane < nw ? st.red_i[32 + lane] : 0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            argmax_step(wv, wi, wn, __shfl_xor_sync(0xffffffffu, wv, o), __shfl_xor_sync(0xffffffffu, wi, o),
-                        __shfl_xor_sync(0xffffffffu, wn, o));
-        if (lane == 0) {
-            st.red_v[64] = wv;
-            st.red_i[64] = wi;
-            st.red_i[65] = wn;
+    float s = 0.f;
+    if ((d & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(v)) & 15) == 0) {
+        const float4* x4 = reinterpret_cast<const float4*>(x);
+        const float4* v4 = reinterpret_cast<const float4*>(v);
+        for (int k = 0; k < (d >> 2); ++k) {
+            const float4 a = x4[k], b = v4[k];
+            float t = a.x - b.x;
+            s = fmaf(t, t, s);
+            t = a.y - b.y;
+            s = fmaf(t, t, s);
+            t = a.z - b.z;
+            s = fmaf(t, t, s);
+            t = a.w - b.w;
+            s = fmaf(t, t, s);
+        }
+    } else {
+        for (int k = 0; k < d; ++k) {
+            const float t = x[k] - v[k];
+            s = fmaf(t, t, s);
         }
     }
-    __syncthreads();
-    out_v = st.red_v[64];
-    out_i = st.red_i[64];
-    if (out_cnt) *out_cnt = st.red_i[65];
-    __syncthreads();
-}
-
-// Euclidean distance of item r to vector v (length d), one warp.
-__device__ __forceinline__ float warp_dist(const float* __restrict__ x, const float* __restrict__ v, int d)
-{
-    const int lane = threadIdx.x & 31;
-    float s = 0.f;
-    for (int k = lane; k < d; k += 32) {
-        const float t = x[k] - v[k];
-        s = fmaf(t, t, s);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return sqrtf(s);
 }
 
-// centroid of group g into cen (d floats, global scratch owned by the block): for
-// d <= blockDim / 2 the items are split over blockDim / d thread groups (thread t adds
-// dimension t % d of items t / d, t / d + H, ...) and the partial sums combined in
-// shared memory; any summation order gives a valid centre (radii are measured from it)
-__device__ void group_centroid(BisectState& st, const float* __restrict__ src, int nitems, int d, int g,
-                               float* __restrict__ cen)
+// block-wide (max value, index) with ties to the smaller index; result in st.pick / st.pick_v
+__device__ __forceinline__ void cover_argmax(CoverState& st, float v, int i)
 {
-    const int H = d <= (int)blockDim.x / 2 ? (int)blockDim.x / d : 1;
-    if (H > 1) {
-        const int k = threadIdx.x % d, h = threadIdx.x / d;
-        float s = 0.f;
-        int cnt = 0;
-        if (h < H)
-            for (int r = h; r < nitems; r += H)
-                if (st.label[r] == g) {
-                    s += src[(int64_t)r * d + k];
-                    ++cnt;
-                }
-        st.part[threadIdx.x] = s;
-        st.pcnt[threadIdx.x] = cnt;
-        __syncthreads();
-        if ((int)threadIdx.x < d) {
-            float t = 0.f;
-            int c = 0;
-            for (int q = 0; q < H; ++q) {
-                t += st.part[q * d + k];
-                c += st.pcnt[q * d + k];
-            }
-            cen[k] = c ? t / (float)c : 0.f;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (ov > v || (ov == v && oi < i)) {
+            v = ov;
+            i = oi;
         }
-        __syncthreads();
-        return;
     }
-    for (int k = threadIdx.x; k < d; k += blockDim.x) {
-        float s = 0.f;
-        int cnt = 0;
-        for (int r = 0; r < nitems; ++r)
-            if (st.label[r] == g) {
-                s += src[(int64_t)r * d + k];
-                ++cnt;
-            }
-        cen[k] = cnt ? s / (float)cnt : 0.f;
+    if (lane == 0) {
+        st.red_v[warp] = v;
+        st.red_i[warp] = i;
     }
     __syncthreads();
-}
-
-// radius of group g around cen: max over items of |x - cen| + irad (irad may be null)
-__device__ void group_radius(BisectState& st, const float* __restrict__ src, const float* __restrict__ irad,
-                             int nitems, int d, int g, const float* __restrict__ cen)
-{
-    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < nitems; r += nw) {
-        if (st.label[r] != g) continue;  // warp-uniform
-        const float dd = warp_dist(src + (int64_t)r * d, cen, d);
-        if ((threadIdx.x & 31) == 0) st.dist[r] = dd + (irad ? irad[r] : 0.f);
-    }
-    __syncthreads();
-    float best = -1.f;
-    int bi = -1, cnt = 0;
-    for (int r = threadIdx.x; r < nitems; r += blockDim.x)
-        if (st.label[r] == g) {
-            ++cnt;
-            if (st.dist[r] > best) { best = st.dist[r]; bi = r; }
-        }
-    float v;
-    int i, total;
-    block_argmax(st, best, bi, v, i, cnt, &total);
     if (threadIdx.x == 0) {
-        st.rad[g] = v;
-        st.far_idx[g] = i;
-        st.count[g] = total;
+        float bv = st.red_v[0];
+        int bi = st.red_i[0];
+        for (int w = 1; w < kCoverThreads / 32; ++w)
+            if (st.red_v[w] > bv || (st.red_v[w] == bv && st.red_i[w] < bi)) {
+                bv = st.red_v[w];
+                bi = st.red_i[w];
+            }
+        st.pick = bi;
+        st.pick_v = bv;
     }
     __syncthreads();
 }
 
-// Splits items into up to kBalls groups; centres written to cen[kBalls][d].
-__device__ void bisect(BisectState& st, const float* __restrict__ src, const float* __restrict__ irad, int nitems,
-                       int d, float* __restrict__ cen)
+// Up to K groups of the n items; centres into cen[K][d] (global, owned by the block),
+// radii into rad[K] (-1: no group).  `cbuf` is d floats of shared memory for the centroid.
+__device__ void cover_groups(CoverState& st, const float* __restrict__ src, const float* __restrict__ irad, int n,
+                             int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ cen,
+                             float* __restrict__ rad)
 {
-    for (int r = threadIdx.x; r < nitems; r += blockDim.x) st.label[r] = 0;
-    if (threadIdx.x == 0) st.ngroups = 1;
+    const int t = threadIdx.x;
+    const bool mine = t < n;
+    const float* xr = src + (int64_t)(mine ? t : 0) * d;
+    const float ir = (mine && irad) ? irad[t] : 0.f;
+    // centroid of all items
+    for (int k = t; k < d; k += blockDim.x) {
+        float a = 0.f;
+        for (int r = 0; r < n; ++r) a += src[(int64_t)r * d + k];
+        cbuf[k] = n > 0 ? a / (float)n : 0.f;
+    }
+    if (t < kCoverMaxBalls) {
+        st.rad_bits[t] = 0u;
+        st.count[t] = 0;
+    }
     __syncthreads();
-    group_centroid(st, src, nitems, d, 0, cen);
-    group_radius(st, src, irad, nitems, d, 0, cen);
-    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    while (st.ngroups < kBalls) {
-        // group with the largest radius that can still be split
-        int g = -1;
-        float gr = 0.f;
-        for (int k = 0; k < st.ngroups; ++k)
-            if (st.count[k] >= 2 && st.rad[k] > gr) { gr = st.rad[k]; g = k; }
-        if (g < 0) break;
-        const int a = st.far_idx[g];
-        // b = farthest (by centre distance) from a within g
-        for (int r = warp; r < nitems; r += nw) {
-            if (st.label[r] != g) continue;
-            const float dd = warp_dist(src + (int64_t)r * d, src + (int64_t)a * d, d);
-            if ((threadIdx.x & 31) == 0) st.dist[r] = dd;
+    float dm = mine ? row_dist(xr, cbuf, d) + ir : -1.f;
+    cover_argmax(st, dm, t);
+    int ng = 0;
+    int lab = 0;
+    for (; ng < K && n > 0; ++ng) {
+        const int j = st.pick;
+        if (ng > 0 && !(st.pick_v > 0.f)) break;  // every item coincides with a centre
+        if (mine) {
+            const float dj = row_dist(xr, src + (int64_t)j * d, d) + ir;
+            if (ng == 0 || dj < dm) {
+                dm = dj;
+                lab = ng;
+            }
         }
-        __syncthreads();
-        float best = -1.f;
-        int bi = -1;
-        for (int r = threadIdx.x; r < nitems; r += blockDim.x)
-            if (st.label[r] == g && st.dist[r] > best) { best = st.dist[r]; bi = r; }
-        float v;
-        int b;
-        block_argmax(st, best, bi, v, b, 0, nullptr);
-        if (b < 0 || b == a || v <= 0.f) {
-            // nothing to split: mark the group unsplittable
-            if (threadIdx.x == 0) st.count[g] = 1;
-            __syncthreads();
-            continue;
-        }
-        const int ng = st.ngroups;
-        for (int r = warp; r < nitems; r += nw) {
-            if (st.label[r] != g) continue;
-            const float db = warp_dist(src + (int64_t)r * d, src + (int64_t)b * d, d);
-            if ((threadIdx.x & 31) == 0 && db < st.dist[r]) st.label[r] = ng;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) st.ngroups = ng + 1;
-        __syncthreads();
-        group_centroid(st, src, nitems, d, g, cen + (int64_t)g * d);
-        group_radius(st, src, irad, nitems, d, g, cen + (int64_t)g * d);
-        group_centroid(st, src, nitems, d, ng, cen + (int64_t)ng * d);
-        group_radius(st, src, irad, nitems, d, ng, cen + (int64_t)ng * d);
-        if (st.count[ng] == 0 || st.count[g] == 0) {
-            // degenerate split (all on one side): undo and stop splitting this group
-            for (int r = threadIdx.x; r < nitems; r += blockDim.x)
-                if (st.label[r] == ng) st.label[r] = g;
-            __syncthreads();
-            if (threadIdx.x == 0) st.ngroups = ng;
-            __syncthreads();
-            group_centroid(st, src, nitems, d, g, cen + (int64_t)g * d);
-            group_radius(st, src, irad, nitems, d, g, cen + (int64_t)g * d);
-            if (threadIdx.x == 0) st.count[g] = 1;
-            __syncthreads();
+        if (ng + 1 < K) cover_argmax(st, mine ? dm : -1.f, t);
+    }
+    if (mine) st.label[t] = lab;
+    __syncthreads();
+    // group centroids (thread k sums dimension k over the group's items), then radii
+    for (int g = 0; g < ng; ++g) {
+        for (int k = t; k < d; k += blockDim.x) {
+            float a = 0.f;
+            int c = 0;
+            for (int r = 0; r < n; ++r)
+                if (st.label[r] == g) {
+                    a += src[(int64_t)r * d + k];
+                    ++c;
+                }
+            cen[(int64_t)g * d + k] = c ? a / (float)c : 0.f;
         }
     }
+    __syncthreads();
+    if (mine) {
+        const float rr = row_dist(xr, cen + (int64_t)lab * d, d) + ir;
+        atomicMax(&st.rad_bits[lab], __float_as_uint(rr));
+        atomicAdd(&st.count[lab], 1);
+    }
+    __syncthreads();
+    if (t < K) rad[t] = (t < ng && st.count[t] > 0) ? __uint_as_float(st.rad_bits[t]) * grow + 1e-30f : -1.f;
+    __syncthreads();
 }
 
-// One block per tile.  Output: centres [T][kBalls][d], radii [T][kBalls] (-1 = unused).
-// With staged = true the tile's rows are first copied to shared memory (kTile * d
-// floats of dynamic shared memory), which every pass of the bisection then reads.
-__global__ void __launch_bounds__(256) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d, float grow,
-                                                    bool staged, float* __restrict__ cen, float* __restrict__ rad)
+// One block per tile.  Output: centres [T][kTileBalls][d], radii [T][kTileBalls] (-1 =
+// unused).  With staged = true the tile's rows are first copied to shared memory, which
+// every pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), plus
+// kTile * d floats when staged.
+__global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d,
+                                                              float grow, bool staged, float* __restrict__ cen,
+                                                              float* __restrict__ rad)
 {
-    __shared__ BisectState st;
-    extern __shared__ __align__(16) float tile_rows[];
+    __shared__ CoverState st;
+    extern __shared__ __align__(16) float dsm[];
+    float* cbuf = dsm;
+    float* tile_rows = dsm + ((d + 3) & ~3);
     const int64_t t = blockIdx.x;
     const int64_t r0 = t * kTile;
     const int nitems = (int)min((int64_t)kTile, n - r0);
-    float* mycen = cen + t * kBalls * d;
     const float* src = Xs + r0 * d;
     if (staged) {
         const int total = nitems * d;
@@ -344,45 +280,43 @@ __global__ void __launch_bounds__(256) k_tile_balls(const float* __restrict__ Xs
         __syncthreads();
         src = tile_rows;
     }
-    bisect(st, src, nullptr, nitems, d, mycen);
-    if (threadIdx.x < kBalls)
-        rad[t * kBalls + threadIdx.x] = threadIdx.x < st.ngroups ? st.rad[threadIdx.x] * grow + 1e-30f : -1.f;
+    cover_groups(st, src, nullptr, nitems, d, kTileBalls, grow, cbuf, cen + t * kTileBalls * d,
+                 rad + t * kTileBalls);
 }
 
-// One block per super-tile: balls over the (up to kSuper * kBalls) valid tile balls.
-__global__ void __launch_bounds__(256) k_super_balls(const float* __restrict__ tcen, const float* __restrict__ trad,
-                                                     int64_t T, int d, float grow, float* __restrict__ work,
-                                                     float* __restrict__ scen, float* __restrict__ srad)
+// One block per super-tile: kSuperBalls balls over its tiles' valid balls (items with
+// their radii).  Dynamic shared memory: d floats.
+__global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __restrict__ tcen,
+                                                               const float* __restrict__ trad, int64_t T, int d,
+                                                               float grow, float* __restrict__ work,
+                                                               float* __restrict__ scen, float* __restrict__ srad)
 {
-    __shared__ BisectState st;
-    __shared__ float irad[kSuper * kBalls];
+    __shared__ CoverState st;
+    __shared__ float irad[kSuper * kTileBalls];
+    __shared__ int src_ball[kSuper * kTileBalls];
     __shared__ int nvalid;
+    extern __shared__ __align__(16) float dsm[];
     const int64_t s = blockIdx.x;
     const int64_t t0 = s * kSuper, t1 = min(T, t0 + kSuper);
-    float* items = work + s * (int64_t)kSuper * kBalls * d;  // compacted valid ball centres
+    float* items = work + s * (int64_t)kSuper * kTileBalls * d;  // compacted valid ball centres
     if (threadIdx.x == 0) {
         int m = 0;
         for (int64_t t = t0; t < t1; ++t)
-            for (int k = 0; k < kBalls; ++k)
-                if (trad[t * kBalls + k] >= 0.f) irad[m++] = trad[t * kBalls + k];
+            for (int k = 0; k < kTileBalls; ++k)
+                if (trad[t * kTileBalls + k] >= 0.f) {
+                    irad[m] = trad[t * kTileBalls + k];
+                    src_ball[m] = (int)((t - t0) * kTileBalls + k);
+                    ++m;
+                }
         nvalid = m;
     }
     __syncthreads();
-    // copy valid centres (same order as irad)
-    {
-        int m = 0;
-        for (int64_t t = t0; t < t1; ++t)
-            for (int k = 0; k < kBalls; ++k) {
-                if (trad[t * kBalls + k] < 0.f) continue;
-                for (int j = threadIdx.x; j < d; j += blockDim.x)
-                    items[(int64_t)m * d + j] = tcen[(t * kBalls + k) * (int64_t)d + j];
-                ++m;
-            }
-    }
+    const int m = nvalid;
+    for (int i = 0; i < m; ++i)
+        for (int j = threadIdx.x; j < d; j += blockDim.x)
+            items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
     __syncthreads();
-    bisect(st, items, irad, nvalid, d, scen + s * kBalls * d);
-    if (threadIdx.x < kBalls)
-        srad[s * kBalls + threadIdx.x] = threadIdx.x < st.ngroups ? st.rad[threadIdx.x] * grow + 1e-30f : -1.f;
+    cover_groups(st, items, irad, m, d, kSuperBalls, grow, dsm, scen + s * kSuperBalls * d, srad + s * kSuperBalls);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -396,7 +330,7 @@ __global__ void __launch_bounds__(256) k_super_close(const float* __restrict__ s
 {
     __shared__ __align__(16) DistSmem sm;
     const int64_t r0 = (int64_t)blockIdx.x * kDRows, c0 = (int64_t)blockIdx.y * kDCols;
-    if (c0 + kDCols <= r0 - kBalls) return;  // strictly below the diagonal of owners
+    if (c0 + kDCols <= r0 - kSuperBalls) return;  // strictly below the diagonal of owners
     float acc[4][4];
     dist_block(sm, scen, nullptr, r0, NB, d, scen, c0, NB, acc);
     const int ty = threadIdx.x >> 3, tx = threadIdx.x & 7;
@@ -410,7 +344,7 @@ __global__ void __launch_bounds__(256) k_super_close(const float* __restrict__ s
         for (int c = 0; c < 4; ++c) {
             const int64_t col = c0 + tx * 4 + c;
             if (col >= NB) continue;
-            const int64_t I = row / kBalls, J = col / kBalls;
+            const int64_t I = row / kSuperBalls, J = col / kSuperBalls;
             if (I > J) continue;
             const float rc = srad[col];
             if (rc < 0.f) continue;
@@ -441,26 +375,52 @@ __global__ void k_bitmap_pairs(const uint32_t* __restrict__ bitmap, int64_t S, i
     }
 }
 
-// Level 2: 64 threads per surviving super pair, four super pairs per block.  Thread
-// (ti, tj) owns tile pair (ta0 + ti, tb0 + tj) and its kBalls x kBalls ball pairs; the
-// two super-tiles' ball centres are staged in shared memory kDC dimensions at a time,
-// transposed so that one float4 load feeds four balls.  A tile pair survives when any
-// of its ball pairs is close; each distance is the sequential fmaf sum over the
-// dimensions, as at the super level.
-constexpr int kNB = kSuper * kBalls;  // balls per super-tile
-constexpr int kDC = 32;               // dimensions per staged chunk
-constexpr int kSPB = 4;               // super pairs per block
+// The bitmap's pairs in row-major (I, J) order: popcount per word, an exclusive scan,
+// then each word writes its pairs at its offset (so consecutive pairs share I).
+__global__ void k_bitmap_count(const uint32_t* __restrict__ bitmap, int64_t words, int32_t* __restrict__ cnt)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x)
+        cnt[w] = __popc(bitmap[w]);
+}
 
-__global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ supers,
-                                                    const unsigned long long* __restrict__ nsup_ptr,
-                                                    unsigned long long sup_cap, const float* __restrict__ tcen,
-                                                    const float* __restrict__ trad, int64_t T, int d, float eps_p,
-                                                    float shrink, int2* __restrict__ out,
-                                                    unsigned long long* __restrict__ count, unsigned long long cap)
+__global__ void k_bitmap_emit(const uint32_t* __restrict__ bitmap, int64_t words, int64_t S,
+                              const int32_t* __restrict__ off, int2* __restrict__ out, unsigned long long cap)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < words; w += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t m = bitmap[w];
+        unsigned long long pos = (unsigned long long)off[w];
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            const int64_t bit = w * 32 + b;
+            if (pos < cap) out[pos] = make_int2((int)(bit / S), (int)(bit % S));
+            ++pos;
+        }
+    }
+}
+
+// Level 2: 64 threads per surviving super pair, kSPB super pairs per block.  Thread
+// (ti, tj) owns tile pair (ta0 + ti, tb0 + tj) and its kTileBalls x kTileBalls ball
+// pairs; the two super-tiles' ball centres are staged in shared memory kDC dimensions at
+// a time, transposed so that one float4 load feeds four balls.  A tile pair survives
+// when any of its ball pairs is close; each distance is the sequential fmaf sum over the
+// dimensions, as at the super level.
+constexpr int kNB = kSuper * kTileBalls;  // balls per super-tile
+constexpr int kDC = 32;                   // dimensions per staged chunk
+constexpr int kSPB = 2;                   // super pairs per block
+static_assert(kTileBalls % 4 == 0, "tile balls are staged four at a time");
+
+__global__ void __launch_bounds__(64 * kSPB) k_tile_close(const int2* __restrict__ supers,
+                                                          const unsigned long long* __restrict__ nsup_ptr,
+                                                          unsigned long long sup_cap, const float* __restrict__ tcen,
+                                                          const float* __restrict__ trad, int64_t T, int d,
+                                                          float eps_p, float shrink, int2* __restrict__ out,
+                                                          unsigned long long* __restrict__ count,
+                                                          unsigned long long cap)
 {
     __shared__ __align__(16) float ca[kSPB][kDC][kNB + 4], cb[kSPB][kDC][kNB + 4];
     const unsigned long long nsup = min(*nsup_ptr, sup_cap);
-    const int sp = threadIdx.x >> 6;       // super pair of this block's four
+    const int sp = threadIdx.x >> 6;       // super pair of this block's kSPB
     const int t = threadIdx.x & 63;
     const int ti = t >> 3, tj = t & 7;     // tile pair inside the super pair
     for (unsigned long long w0 = (unsigned long long)blockIdx.x * kSPB; w0 < nsup;
@@ -469,20 +429,20 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
         const bool live = w < nsup;
         const int2 spair = live ? supers[w] : make_int2(0, 0);
         const int64_t ta0 = (int64_t)spair.x * kSuper, tb0 = (int64_t)spair.y * kSuper;
-        float acc[kBalls][kBalls];
+        float acc[kTileBalls][kTileBalls];
 #pragma unroll
-        for (int x = 0; x < kBalls; ++x)
+        for (int x = 0; x < kTileBalls; ++x)
 #pragma unroll
-            for (int y = 0; y < kBalls; ++y) acc[x][y] = 0.f;
+            for (int y = 0; y < kTileBalls; ++y) acc[x][y] = 0.f;
         for (int k0 = 0; k0 < d; k0 += kDC) {
             __syncthreads();
             // stage: kNB balls x kDC dims per side as float4 along the dimension
             for (int idx = t; idx < kNB * (kDC / 4); idx += 64) {
                 const int ball = idx / (kDC / 4), q4 = idx % (kDC / 4), k = k0 + 4 * q4;
-                const int64_t t1 = ta0 + ball / kBalls, t2 = tb0 + ball / kBalls;
+                const int64_t t1 = ta0 + ball / kTileBalls, t2 = tb0 + ball / kTileBalls;
                 float4 va = make_float4(0.f, 0.f, 0.f, 0.f), vb = va;
                 if (live && t1 < T) {
-                    const float* src = tcen + (t1 * kBalls + ball % kBalls) * (int64_t)d;
+                    const float* src = tcen + (t1 * kTileBalls + ball % kTileBalls) * (int64_t)d;
                     if (k + 3 < d && (d & 3) == 0) va = *reinterpret_cast<const float4*>(src + k);
                     else {
                         va.x = k < d ? src[k] : 0.f;
@@ -492,7 +452,7 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
                     }
                 }
                 if (live && t2 < T) {
-                    const float* src = tcen + (t2 * kBalls + ball % kBalls) * (int64_t)d;
+                    const float* src = tcen + (t2 * kTileBalls + ball % kTileBalls) * (int64_t)d;
                     if (k + 3 < d && (d & 3) == 0) vb = *reinterpret_cast<const float4*>(src + k);
                     else {
                         vb.x = k < d ? src[k] : 0.f;
@@ -512,15 +472,20 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
             }
             __syncthreads();
             const int kk_end = min(kDC, d - k0);
-#pragma unroll 4
+#pragma unroll 2
             for (int kk = 0; kk < kk_end; ++kk) {
-                const float4 a4 = *reinterpret_cast<const float4*>(&ca[sp][kk][ti * kBalls]);
-                const float4 b4 = *reinterpret_cast<const float4*>(&cb[sp][kk][tj * kBalls]);
-                const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+                float av[kTileBalls], bv[kTileBalls];
 #pragma unroll
-                for (int x = 0; x < kBalls; ++x)
+                for (int q = 0; q < kTileBalls / 4; ++q) {
+                    const float4 a4 = *reinterpret_cast<const float4*>(&ca[sp][kk][ti * kTileBalls + 4 * q]);
+                    const float4 b4 = *reinterpret_cast<const float4*>(&cb[sp][kk][tj * kTileBalls + 4 * q]);
+                    av[4 * q] = a4.x; av[4 * q + 1] = a4.y; av[4 * q + 2] = a4.z; av[4 * q + 3] = a4.w;
+                    bv[4 * q] = b4.x; bv[4 * q + 1] = b4.y; bv[4 * q + 2] = b4.z; bv[4 * q + 3] = b4.w;
+                }
 #pragma unroll
-                    for (int y = 0; y < kBalls; ++y) {
+                for (int x = 0; x < kTileBalls; ++x)
+#pragma unroll
+                    for (int y = 0; y < kTileBalls; ++y) {
                         const float df = av[x] - bv[y];
                         acc[x][y] = fmaf(df, df, acc[x][y]);
                     }
@@ -530,11 +495,11 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
         bool keep = false;
         if (live && i < T && j < T && i <= j) {
 #pragma unroll
-            for (int x = 0; x < kBalls; ++x) {
-                const float ra = trad[i * kBalls + x];
+            for (int x = 0; x < kTileBalls; ++x) {
+                const float ra = trad[i * kTileBalls + x];
 #pragma unroll
-                for (int y = 0; y < kBalls; ++y) {
-                    const float rb = trad[j * kBalls + y];
+                for (int y = 0; y < kTileBalls; ++y) {
+                    const float rb = trad[j * kTileBalls + y];
                     if (ra >= 0.f && rb >= 0.f && sqrtf(acc[x][y]) * shrink <= eps_p + ra + rb) keep = true;
                 }
             }
@@ -551,9 +516,10 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
     }
 }
 
-// Level 2 on the tensor cores (d <= 256): one warp per surviving super pair computes the
-// 32 x 32 Gram block of the two super-tiles' BF16 ball centres with mma.sync (m16n8k16,
-// FP32 accumulation) and keeps a tile pair when one of its 4 x 4 ball pairs passes
+// Level 2 on the tensor cores (d <= 256): four warps per surviving super pair compute
+// the kSB x kSB Gram block of the two super-tiles' BF16 ball centres with mma.sync
+// (m16n8k16, FP32 accumulation; warp w takes row balls 16 w .. 16 w + 15) and keep a
+// tile pair when one of its kTileBalls x kTileBalls ball pairs passes
 //
 //     n_a + n_b - 2 g  <=  (eps' + r_a + r_b + a_a + a_b)^2 + q_a + q_b   (+ relative slack)
 //
@@ -565,118 +531,99 @@ __global__ void __launch_bounds__(256) k_tile_close(const int2* __restrict__ sup
 // for both operands (a dot product does not depend on it) so that every lane fetches
 // its fragments with 16-byte loads: lane (g, t) reads columns 8t .. 8t + 7, which feed
 // k-slots {2t, 2t+1, 2t+8, 2t+9} of two consecutive k-steps.
-constexpr int kSB = kSuper * kBalls;  // balls per super-tile (32)
+constexpr int kSB = kSuper * kTileBalls;  // balls per super-tile (64)
+static_assert(kTileBalls == 8 && kSB == 64, "the warp layout of k_tile_close_mma: 16 row balls = 2 tiles per warp");
 
-__global__ void __launch_bounds__(256) k_tile_close_mma(const int2* __restrict__ supers,
+// KP = dp / 32 k-groups.  Block b takes the contiguous range b of the super-pair list
+// (row-major, so consecutive pairs share their row super-tile) and keeps the row
+// super-tile's A fragments in registers while it lasts.
+template <int KP>
+__global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__ supers,
                                                         const unsigned long long* __restrict__ nsup_ptr,
                                                         unsigned long long sup_cap, const uint4* __restrict__ cb,
-                                                        const float4* __restrict__ binfo, int dp, int64_t T,
-                                                        float eps_p, float kappa, int2* __restrict__ out,
+                                                        const float4* __restrict__ binfo, int64_t T, float eps_p,
+                                                        float kappa, int2* __restrict__ out,
                                                         unsigned long long* __restrict__ count, unsigned long long cap)
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    constexpr int rowq = 4 * KP;  // uint4 per BF16 row (dp / 8)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
     const unsigned long long nsup = min(*nsup_ptr, sup_cap);
-    const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-    const int rowq = dp / 8;  // uint4 per BF16 row
-    for (unsigned long long w = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nsup; w += nw) {
+    const unsigned long long per = (nsup + gridDim.x - 1) / gridDim.x;
+    const unsigned long long w0 = (unsigned long long)blockIdx.x * per, w1 = min(nsup, w0 + per);
+    int cur = -1;
+    uint4 a0[KP], a1[KP];
+    float4 x0 = make_float4(0.f, 0.f, 0.f, -1.f), x1 = x0;
+    for (unsigned long long w = w0; w < w1; ++w) {
         const int2 sp = supers[w];
-        const int64_t ra = (int64_t)sp.x * kSB, rb = (int64_t)sp.y * kSB;  // first ball row of each side
-        float acc[2][4][4];
+        const int64_t ra = (int64_t)sp.x * kSB + 16 * warp, rb = (int64_t)sp.y * kSB;  // first ball rows
+        if (sp.x != cur) {
+            const uint4* pa = cb + (ra + g) * rowq + t;
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
-        const uint4* pa = cb + (ra + g) * rowq + t;
-        const uint4* pb = cb + (rb + g) * rowq + t;
-#pragma unroll 1
-        for (int kp = 0; kp < dp / 32; ++kp) {
-            uint4 a[2][2], b[4];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) a[mt][h] = pa[(16 * mt + 8 * h) * rowq + 4 * kp];
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) b[nt] = pb[(8 * nt) * rowq + 4 * kp];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                for (int nt = 0; nt < 4; ++nt) {
-                    mma_bf16_16816(acc[mt][nt], a[mt][0].x, a[mt][1].x, a[mt][0].y, a[mt][1].y, b[nt].x, b[nt].y);
-                    mma_bf16_16816(acc[mt][nt], a[mt][0].z, a[mt][1].z, a[mt][0].w, a[mt][1].w, b[nt].z, b[nt].w);
-                }
+            for (int kp = 0; kp < KP; ++kp) {
+                a0[kp] = pa[4 * kp];
+                a1[kp] = pa[8 * rowq + 4 * kp];
+            }
+            x0 = binfo[ra + g];
+            x1 = binfo[ra + 8 + g];
+            cur = sp.x;
         }
-        // acc[mt][nt][2h + e] = ball row 16 mt + 8 h + g, ball column 8 nt + 2 t + e; their tiles
-        // are row tile 4 mt + 2 h + g / 4 and column tile 2 nt + t / 2 of the super pair
-        float4 ir[4];
+        float acc[8][4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) ir[k] = binfo[ra + 8 * k + g];  // k = 2 mt + h
-        uint32_t msk = 0;  // bit 4 (2 mt + h) + nt
+        for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
+            for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+        const uint4* pb = cb + (rb + g) * rowq + t;
+#pragma unroll
+        for (int kp = 0; kp < KP; ++kp) {
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint4 b = pb[(8 * nt) * rowq + 4 * kp];
+                mma_bf16_16816(acc[nt], a0[kp].x, a1[kp].x, a0[kp].y, a1[kp].y, b.x, b.y);
+                mma_bf16_16816(acc[nt], a0[kp].z, a1[kp].z, a0[kp].w, a1[kp].w, b.z, b.w);
+            }
+        }
+        // acc[nt][2h + e] = row ball 16 warp + 8 h + g, column ball 8 nt + 2 t + e: row tile
+        // 2 warp + h, column tile nt of the super pair
+        uint32_t msk = 0;  // bit 8 h + nt
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const float4 y = binfo[rb + 8 * nt + 2 * t + e];
 #pragma unroll
-                for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const float4 x = ir[2 * mt + h];
-                        const float D = fmaf(-2.f, acc[mt][nt][2 * h + e], x.x + y.x);
-                        const float E = eps_p + x.w + y.w + x.y + y.y;
-                        const float R = fmaf(E, E, x.z + y.z);
-                        const bool keep = x.w >= 0.f && y.w >= 0.f && D <= R + kappa * (x.x + y.x + R);
-                        msk |= (keep ? 1u : 0u) << (4 * (2 * mt + h) + nt);
-                    }
-            }
-        // OR over the lanes holding the other balls of the same tiles (g % 4 and t % 2)
-        msk |= __shfl_xor_sync(0xffffffffu, msk, 1);
-        msk |= __shfl_xor_sync(0xffffffffu, msk, 4);
-        msk |= __shfl_xor_sync(0xffffffffu, msk, 8);
-        // lanes (g % 4 == 0, t % 2 == 0) report: row tiles g / 4 + 2 k, column tiles t / 2 + 2 nt
-        const bool reporter = (lane & 13) == 0;
-        uint32_t mine = 0;
-        if (reporter) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-#pragma unroll
-                for (int nt = 0; nt < 4; ++nt) {
-                    const int64_t i = (int64_t)sp.x * kSuper + (g >> 2) + 2 * k;
-                    const int64_t j = (int64_t)sp.y * kSuper + (t >> 1) + 2 * nt;
-                    if (((msk >> (4 * k + nt)) & 1u) && i < T && j < T && i <= j) mine |= 1u << (4 * k + nt);
+                for (int h = 0; h < 2; ++h) {
+                    const float4 x = h ? x1 : x0;
+                    const float D = fmaf(-2.f, acc[nt][2 * h + e], x.x + y.x);
+                    const float E = eps_p + x.w + y.w + x.y + y.y;
+                    const float R = fmaf(E, E, x.z + y.z);
+                    const bool keep = x.w >= 0.f && y.w >= 0.f && D <= R + kappa * (x.x + y.x + R);
+                    msk |= (keep ? 1u : 0u) << (8 * h + nt);
                 }
-        }
-        const int cnt = __popc(mine);
-        int incl = cnt;
+            }
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total == 0) continue;
+        for (int o = 1; o < 32; o <<= 1) msk |= __shfl_xor_sync(0xffffffffu, msk, o);
+        // lane b < 16 reports tile pair (row tile 2 warp + b / 8, column tile b % 8)
+        const int64_t i = (int64_t)sp.x * kSuper + 2 * warp + (lane >> 3);
+        const int64_t j = (int64_t)sp.y * kSuper + (lane & 7);
+        const bool mine = lane < 16 && ((msk >> lane) & 1u) && i < T && j < T && i <= j;
+        const unsigned bal = __ballot_sync(0xffffffffu, mine);
+        if (!bal) continue;
         unsigned long long base = 0;
-        if (lane == 31) base = atomicAdd(count, (unsigned long long)total);
-        base = __shfl_sync(0xffffffffu, base, 31);
-        unsigned long long pos = base + (unsigned long long)(incl - cnt);
-        while (mine) {
-            const int bit = __ffs(mine) - 1;
-            mine &= mine - 1;
-            if (pos < cap)
-                out[pos] = make_int2(sp.x * kSuper + (g >> 2) + 2 * (bit >> 2), sp.y * kSuper + (t >> 1) + 2 * (bit & 3));
-            ++pos;
+        if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (mine) {
+            const unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
+            if (pos < cap) out[pos] = make_int2((int)i, (int)j);
         }
     }
 }
 
 // Items of the persistent Gram kernel.  The pairs are sorted by (row tile, column
 // tile); inside a row they are grouped nt at a time into items {i, j0, j1} (j1 = -1 for
-// a row's last odd pair or nt = 1).  The items are cut into chunks of kSchedChunk and
-// chunk k goes to CTA k mod G: every CTA gets the same number of items (within one
-// chunk), all CTAs work on neighbouring rows at any moment (their B tiles are shared
-// through L2), and a CTA reloads its resident A tile at most once per chunk.  Each
-// CTA's chunks are stored contiguously, so the kernel reads one range per CTA.
+// a row's last odd pair or nt = 1).  The kernel's CTAs take chunks of consecutive items
+// from a device-side queue in item order, so all CTAs work on neighbouring rows at any
+// moment (their B tiles are shared through L2) and a CTA reloads its resident A tile at
+// most once per chunk plus once per row change.
 __global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, uint64_t* __restrict__ keys)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
@@ -713,17 +660,6 @@ __global__ void k_items(const uint64_t* __restrict__ keys, int64_t m, int nt, co
     }
 }
 
-__global__ void k_schedule_scatter(const int4* __restrict__ sorted, int64_t m, int G,
-                                   const unsigned long long* __restrict__ starts, int4* __restrict__ items)
-{
-    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t chunk = p / kSchedChunk;
-        const int g = (int)(chunk % G);
-        const int64_t dest = (int64_t)starts[g] + (chunk / G) * kSchedChunk + p % kSchedChunk;
-        items[dest] = sorted[p];
-    }
-}
-
 // ------------------------------------------------------------------------------------------------
 // host
 
@@ -747,21 +683,22 @@ void build_covers(rnng_ctx* c, Layout& L)
 {
     cudaStream_t s = c->stream;
     const float grow = 1.f + L.relerr;
-    c->tile_lo.reserve(sizeof(float) * (size_t)L.T * kBalls * L.d);   // tile ball centres
-    c->tile_hi.reserve(sizeof(float) * (size_t)L.T * kBalls);         // tile ball radii
-    c->super_lo.reserve(sizeof(float) * (size_t)L.S * kBalls * L.d);  // super ball centres
-    c->super_hi.reserve(sizeof(float) * (size_t)L.S * kBalls);        // super ball radii
-    c->pivots.reserve(sizeof(float) * (size_t)L.S * kSuper * kBalls * L.d);  // compaction workspace
-    // tiles staged in shared memory up to 64 dimensions (32 KB: the bisection's many block
-    // barriers need several blocks per SM, so larger tiles read through L1 instead)
-    const bool staged = L.d <= 64;
-    const size_t tsm = staged ? sizeof(float) * kTile * (size_t)L.d : 0;
-    if (staged) RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-    k_tile_balls<<<(unsigned)L.T, 256, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, c->tile_lo.as<float>(),
-                                                 c->tile_hi.as<float>()); ++c->launches;
-    k_super_balls<<<(unsigned)L.S, 256, 0, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d, grow,
-                                                c->pivots.as<float>(), c->super_lo.as<float>(),
-                                                c->super_hi.as<float>()); ++c->launches;
+    c->tile_lo.reserve(sizeof(float) * (size_t)L.T * kTileBalls * L.d);    // tile ball centres
+    c->tile_hi.reserve(sizeof(float) * (size_t)L.T * kTileBalls);          // tile ball radii
+    c->super_lo.reserve(sizeof(float) * (size_t)L.S * kSuperBalls * L.d);  // super ball centres
+    c->super_hi.reserve(sizeof(float) * (size_t)L.S * kSuperBalls);        // super ball radii
+    c->pivots.reserve(sizeof(float) * (size_t)L.S * kSuper * kTileBalls * L.d);  // compaction workspace
+    // tiles staged in shared memory up to 128 dimensions (64 KB; larger tiles read through L1)
+    const bool staged = L.d <= 128;
+    const size_t csm = sizeof(float) * (size_t)((L.d + 3) & ~3);
+    const size_t tsm = csm + (staged ? sizeof(float) * kTile * (size_t)L.d : 0);
+    RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+    k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, c->tile_lo.as<float>(),
+                                                           c->tile_hi.as<float>()); ++c->launches;
+    k_super_balls<<<(unsigned)L.S, kCoverThreads, csm, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d,
+                                                            grow, c->pivots.as<float>(), c->super_lo.as<float>(),
+                                                            c->super_hi.as<float>()); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 
@@ -773,7 +710,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
     const float eps_p = widened_radius(L.radius, L.d);
     const float shrink = 1.f - L.relerr;
     // level 1: bitmap of close super-tile pairs
-    const int64_t NB = L.S * kBalls;
+    const int64_t NB = L.S * kSuperBalls;
     const int64_t words = (L.S * L.S + 31) / 32;
     c->aux6.reserve(sizeof(uint32_t) * (size_t)words);
     uint32_t* bitmap = c->aux6.as<uint32_t>();
@@ -781,19 +718,37 @@ void prune_covers(rnng_ctx* c, Layout& L)
     dim3 g1((unsigned)ceil_div(NB, kDRows), (unsigned)ceil_div(NB, kDCols));
     k_super_close<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), NB, L.d, eps_p, shrink, bitmap,
                                      L.S); ++c->launches;
-    unsigned long long sup_cap = std::max<unsigned long long>(4096, (unsigned long long)L.S * 64);
-    sup_cap = std::min<unsigned long long>(sup_cap, (unsigned long long)L.S * (L.S + 1) / 2);
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        c->super_list.reserve(sizeof(int2) * sup_cap);
-        RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
-        k_bitmap_pairs<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(words, 256), (int64_t)c->num_sms * 8)),
-                         256, 0, s>>>(bitmap, L.S, c->super_list.as<int2>(), cnt, sup_cap); ++c->launches;
-        unsigned long long got = 0;
-        RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
+    const unsigned bgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(words, 256), (int64_t)c->num_sms * 8));
+    if ((unsigned long long)L.S * (L.S + 1) / 2 < (1ull << 31)) {
+        // row-major pair list: per-word counts, a scan, then each word's pairs at its offset
+        c->sched.reserve(sizeof(int32_t) * 2 * (size_t)(words + 1));
+        int32_t* wc = c->sched.as<int32_t>();
+        int32_t* wo = wc + words + 1;
+        k_bitmap_count<<<bgrid, 256, 0, s>>>(bitmap, words, wc); ++c->launches;
+        RNNG_CUDA(cudaMemsetAsync(wc + words, 0, sizeof(int32_t), s));
+        exclusive_scan_i32(c, wc, wo, words + 1);
+        int32_t total = 0;
+        RNNG_CUDA(cudaMemcpyAsync(&total, wo + words, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
         RNNG_CUDA(cudaStreamSynchronize(s));
-        L.super_pairs = got;
-        if (got <= sup_cap) break;
-        sup_cap = got;
+        L.super_pairs = (unsigned long long)total;
+        c->super_list.reserve(sizeof(int2) * std::max<unsigned long long>(1, L.super_pairs));
+        k_bitmap_emit<<<bgrid, 256, 0, s>>>(bitmap, words, L.S, wo, c->super_list.as<int2>(), L.super_pairs);
+        ++c->launches;
+        RNNG_CUDA(cudaMemcpyAsync(cnt, &L.super_pairs, sizeof(unsigned long long), cudaMemcpyHostToDevice, s));
+    } else {
+        unsigned long long sup_cap = std::max<unsigned long long>(4096, (unsigned long long)L.S * 64);
+        sup_cap = std::min<unsigned long long>(sup_cap, (unsigned long long)L.S * (L.S + 1) / 2);
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            c->super_list.reserve(sizeof(int2) * sup_cap);
+            RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+            k_bitmap_pairs<<<bgrid, 256, 0, s>>>(bitmap, L.S, c->super_list.as<int2>(), cnt, sup_cap); ++c->launches;
+            unsigned long long got = 0;
+            RNNG_CUDA(cudaMemcpyAsync(&got, cnt, sizeof(got), cudaMemcpyDeviceToHost, s));
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            L.super_pairs = got;
+            if (got <= sup_cap) break;
+            sup_cap = got;
+        }
     }
     // level 2: tile pairs inside the surviving super pairs
     const unsigned long long tile_cap =
@@ -809,7 +764,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
     bool tc = bf16_supported(L.d);
     const int dp = (int)ceil_div(L.d, 64) * 64;
     if (tc) {
-        const int64_t nb = L.T * kBalls, nb_pad = L.S * kSB;
+        const int64_t nb = L.T * kTileBalls, nb_pad = L.S * kSB;
         c->ball_b16.reserve(sizeof(__nv_bfloat16) * (size_t)nb_pad * dp);
         c->ball_info.reserve(sizeof(float4) * (size_t)nb_pad);
         const float widen = prepare_ball_bf16(c, L, c->tile_lo.as<float>(), c->tile_hi.as<float>(), nb, nb_pad, eps_p,
@@ -821,12 +776,21 @@ void prune_covers(rnng_ctx* c, Layout& L)
     if (tc) {
         const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
         const unsigned wgrid = (unsigned)std::max<unsigned long long>(
-            1, std::min<unsigned long long>((L.super_pairs + 7) / 8, (unsigned long long)c->num_sms * 8));
-        k_tile_close_mma<<<wgrid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->ball_b16.as<uint4>(),
-                                               c->ball_info.as<float4>(), dp, L.T, eps_p, kappa,
-                                               c->pair_list.as<int2>(), cnt + 1, tile_cap); ++c->launches;
+            1, std::min<unsigned long long>(L.super_pairs, (unsigned long long)c->num_sms * 16));
+        auto launch = [&](auto kern) {
+            kern<<<wgrid, 128, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->ball_b16.as<uint4>(),
+                                       c->ball_info.as<float4>(), L.T, eps_p, kappa, c->pair_list.as<int2>(), cnt + 1,
+                                       tile_cap);
+        };
+        switch (dp / 32) {
+            case 2: launch(k_tile_close_mma<2>); break;
+            case 4: launch(k_tile_close_mma<4>); break;
+            case 6: launch(k_tile_close_mma<6>); break;
+            default: launch(k_tile_close_mma<8>); break;
+        }
+        ++c->launches;
     } else {
-        k_tile_close<<<grid, 256, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
+        k_tile_close<<<grid, 64 * kSPB, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->tile_lo.as<float>(),
                                           c->tile_hi.as<float>(), L.T, L.d, eps_p, shrink, c->pair_list.as<int2>(),
                                           cnt + 1, tile_cap); ++c->launches;
     }
@@ -838,7 +802,7 @@ void prune_covers(rnng_ctx* c, Layout& L)
     L.d_tile_pairs = cnt + 1;
 }
 
-void schedule_items(rnng_ctx* c, Layout& L, int max_ctas, int nt)
+void schedule_items(rnng_ctx* c, Layout& L, int nt)
 {
     cudaStream_t s = c->stream;
     const int64_t m = (int64_t)L.tile_pairs;
@@ -849,8 +813,6 @@ void schedule_items(rnng_ctx* c, Layout& L, int max_ctas, int nt)
     // items in (row, column) order
     int64_t ni = 0;
     c->items.reserve(sizeof(int4) * (size_t)mg);
-    c->items_tmp.reserve(sizeof(int4) * (size_t)mg);
-    int4* sorted = c->items_tmp.as<int4>();
     if (m > 0) {
         c->aux6.reserve(sizeof(uint64_t) * 2 * (size_t)m);
         uint64_t* k0 = c->aux6.as<uint64_t>();
@@ -871,32 +833,12 @@ void schedule_items(rnng_ctx* c, Layout& L, int max_ctas, int nt)
         exclusive_scan_i32(c, start, off, m + 1);
         int32_t total = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, off + m, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        k_items<<<grid, 256, 0, s>>>(k1, m, nt, start, off, sorted); ++c->launches;
+        k_items<<<grid, 256, 0, s>>>(k1, m, nt, start, off, c->items.as<int4>()); ++c->launches;
         RNNG_CUDA(cudaStreamSynchronize(s));
         ni = total;
     }
     L.num_items = (unsigned long long)ni;
     L.items = c->items.as<int4>();
-    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(ni, (int64_t)max_ctas));
-    L.sched_G = G;
-    // segment of CTA g: its chunks k = g, g + G, ... (all full but the very last chunk)
-    c->sched.reserve(sizeof(unsigned long long) * (G + 1));
-    unsigned long long* starts = c->sched.as<unsigned long long>();
-    L.sched = starts;
-    const int64_t nchunks = ceil_div(ni, kSchedChunk), tail = ni % kSchedChunk;
-    std::vector<unsigned long long> h(G + 1, 0);
-    for (int g = 0; g < G; ++g) {
-        int64_t size = (nchunks / G + (g < nchunks % G ? 1 : 0)) * kSchedChunk;
-        if (tail > 0 && (nchunks - 1) % G == g) size -= kSchedChunk - tail;
-        h[g + 1] = h[g] + (unsigned long long)size;
-    }
-    RNNG_CUDA(cudaMemcpyAsync(starts, h.data(), sizeof(unsigned long long) * (G + 1), cudaMemcpyHostToDevice, s));
-    if (ni > 0) {
-        const unsigned grid =
-            (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ni, 256), (int64_t)c->num_sms * 8));
-        k_schedule_scatter<<<grid, 256, 0, s>>>(sorted, ni, G, starts, L.items); ++c->launches;
-    }
-    RNNG_CUDA(cudaStreamSynchronize(s));  // h lifetime
 }
 
 }  // namespace rnng

@@ -40,6 +40,7 @@ struct Error {
 // (float bits).
 constexpr int kCounterSlots = 16;
 constexpr int kSlotNonfinite = 13;
+constexpr int kSlotQueue = 7;  // the Gram kernel's work-queue head
 
 // A growable device buffer owned by the context.  Buffers are reused across calls
 // so that steady-state calls do not allocate.
@@ -72,6 +73,17 @@ enum DeviceFault : int {
     FAULT_NONE = 0,
     FAULT_MBAR_TIMEOUT = 1,
     FAULT_QUEUE = 2,
+};
+
+// One row of the Gram kernel's tuning table (rnng_gb300/gram_tuning.json, written by the
+// autotuner rnng_gb300/tune.py): for operands of padded width dp of one kind and at least
+// min_pairs tile pairs, nt column tiles per item, chunk items per queue chunk and at most
+// slots B slots per CTA (0: as many as fit).
+struct GramTune {
+    int kind = 0;               // 0: BF16 L2 tiles, 1: the FP8 edit-distance filter
+    int dp = 0;
+    long long min_pairs = 0;
+    int nt = 0, chunk = 0, slots = 0;
 };
 
 }  // namespace rnng
@@ -108,6 +120,8 @@ struct rnng_ctx {
     double gram_ms = 0.0;       // device time of the Gram kernel launches of the current call
     cudaEvent_t ev[16] = {};
     bool have_events = false;
+    std::vector<rnng::GramTune> gram_table;  // loaded at creation
+    rnng::GramTune gram_force;                // rnng_ctx_set_gram_tuning (0 fields: not forced)
 };
 
 namespace rnng {

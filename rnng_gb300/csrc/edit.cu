@@ -699,7 +699,10 @@ extern "C" int rnng_eps_graph_edit(rnng_ctx* c, const uint8_t* atoms, const int6
                 Le.d = kFilterBytes;
                 Le.pairs = c->pair_list.as<int2>();
                 Le.tile_pairs = (unsigned long long)npairs;
-                schedule_items(c, Le, c->num_sms, 1);
+                const GramTune t = gram_tune(c, 1, kFilterBytes, npairs);
+                Le.gram_chunk = t.chunk;
+                Le.gram_slots = t.slots;
+                schedule_items(c, Le, 1);
                 // thr^2 (as the kernel squares it in FP32) in [2 q K, 2 q K + 1): the integer test
                 // L1 <= 2 q K exactly
                 const float lim = (float)(2 * qf * K);

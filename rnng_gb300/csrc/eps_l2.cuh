@@ -10,11 +10,12 @@ namespace rnng {
 
 constexpr int kTile = 128;          // points per tile (one tcgen05 M=128 / N=128 operand)
 constexpr int kSuper = 8;           // tiles per super-tile in the first pruning level
-constexpr int kBalls = 4;           // balls covering one tile (and one super-tile)
+constexpr int kTileBalls = 8;       // balls covering one tile
+constexpr int kSuperBalls = 16;     // balls covering one super-tile
 constexpr int kFan = 64;            // children per split of the landmark partition
 constexpr int64_t kLeafTarget = 128;  // points per leaf cell
 constexpr int kMaxLevels = 8;       // depth limit of the partition
-constexpr int64_t kSchedChunk = 64;  // consecutive tile pairs a Gram CTA takes at a time
+constexpr int kBf16MinDim = 16;     // BF16 mode evaluates tiles of fewer dimensions with FP32-direct tiles
 
 // Device layout of one epsilon-graph problem after the partition.
 struct Layout {
@@ -29,12 +30,13 @@ struct Layout {
     int2* pairs = nullptr;        // surviving tile pairs (i <= j)
     unsigned long long* d_tile_pairs = nullptr;  // device copy of tile_pairs
     // BF16 Gram items: a row tile with item_tiles column tiles {y, z} (z = -1: none), in
-    // the per-CTA order of the schedule; sched holds the G + 1 range starts
+    // (row, column) order; the kernel's queue hands them out gram_chunk at a time, with at
+    // most gram_slots B slots per CTA (0: as many as fit)
     int4* items = nullptr;
     unsigned long long num_items = 0;
     int item_tiles = 1;
-    unsigned long long* sched = nullptr;
-    int sched_G = 0;
+    int gram_chunk = 64;
+    int gram_slots = 0;
     // build_layout stopped before the partition: the screen found a non-finite input value
     bool nonfinite = false;
     float maxabs = 0.f;  // largest |coordinate| (d <= 256 only)
@@ -97,8 +99,13 @@ float prepare_ball_bf16(rnng_ctx* c, Layout& L, const float* cen, const float* r
                         float eps_p, __nv_bfloat16* out, float4* info);
 void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E);
 bool bf16_supported(int d);
-// Column tiles per Gram item for dimension d (2: N = 256 MMAs, 1: N = 128).
-int gram_item_tiles(int d);
+// Tuning of the Gram kernel for operands of padded width dp (kind 0: BF16 L2 tiles, 1: the
+// FP8 edit filter) over tile_pairs tile pairs: the context's forced values, else the
+// tuning table's row, else the defaults (nt 2 up to dp 128, chunks of 64 items, as many B
+// slots as fit); nt and chunk are adjusted to the compiled kernel forms.
+GramTune gram_tune(rnng_ctx* c, int kind, int dp, int64_t tile_pairs);
+// The tuning table read when a context is created (a missing file leaves it empty).
+void load_gram_table(rnng_ctx* c);
 
 // Filter rows of 0/1 values as E4M3 bytes (0x00 / 0x38), kFilterBytes per row, n_pad rows in
 // the tile order of L: candidate pairs (i < j) of L's scheduled items whose

@@ -16,11 +16,14 @@
 // each candidate is then re-evaluated with the reference's sequential FP32 L2 in a
 // separate kernel: the edge set and every weight are exactly the reference's.
 //
-// Kernel roles (one CTA per SM, persistent over the scheduled items; an item is a row
-// tile with up to two column tiles):
-//   warp 0      TMA producer: the A tile (rows of I, all K-chunks of 64 BF16 = one
-//               128 B swizzle span each) into a resident buffer when I changes, and
-//               the B tiles (rows of J, all K-chunks) into a ring of item slots
+// Kernel roles (one CTA per SM, persistent; an item is a row tile with up to two column
+// tiles; the CTAs pull chunks of consecutive items from a device-side work queue, an
+// atomic head in global memory, so uneven work evens out across the SMs):
+//   warp 0      TMA producer: takes the next chunk from the queue and posts its first
+//               item into a small ring in shared memory for the other roles; loads the
+//               A tile (rows of I, all K-chunks of 64 BF16 = one 128 B swizzle span each)
+//               into a resident buffer when I changes, and the B tiles (rows of J, all
+//               K-chunks) into a ring of item slots
 //   warp 1      MMA issuer: (M=128, N=128 per column tile, K=16) MMAs into one of the
 //               accumulators of 512 TMEM columns, one commit per item
 //   warps 2-17  epilogue, two groups of 8 (one column tile each): 2 warps per TMEM
@@ -34,7 +37,11 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <dlfcn.h>
+
 #include <cmath>
+#include <cstdlib>
+#include <string>
 
 #include "common.cuh"
 #include "eps_l2.cuh"
@@ -45,6 +52,7 @@ constexpr int kChunkK = 64;                         // BF16 elements per K-chunk
 constexpr int kChunkBytes = kTile * kChunkK * 2;    // 16 KB per operand tile per chunk
 constexpr int kMaxDp = 256;                         // padded dimension limit of the BF16 path
 constexpr int kMaxSlots = 8;
+constexpr int kChunkRing = 4;                       // queue chunks posted ahead to the consumers
 constexpr int kAccCols = 128;                       // fp32 accumulator columns (N)
 constexpr int kAccBufs = 4;                         // accumulators in tensor memory
 constexpr int kTmemCols = kAccBufs * kAccCols;      // all 512 columns
@@ -65,21 +73,25 @@ constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared mem
 // nt tiles x kch chunks as the rest of the 227 KB holds.  Operand tiles start on
 // 1024-byte boundaries (128-byte swizzle atoms).
 struct GramSmem {
-    uint32_t colinfo, bars, misc, a_tile, b_ring, slot_bytes, total;
+    uint32_t colinfo, bars, misc, cq, a_tile, b_ring, slot_bytes, total;
     int nslots;
-    static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1;  // a_full/empty, b_full/empty, tfull/tempty, drain
-    __host__ __device__ static GramSmem make(int kch, int nt)
+    // a_full/empty, b_full/empty, tfull/tempty, drain, chunk ring full/empty
+    static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1 + 2 * kChunkRing;
+    // max_slots > 0 caps the B ring (a tuning knob); the ring always holds at least 2 slots
+    __host__ __device__ static GramSmem make(int kch, int nt, int max_slots = 0)
     {
         GramSmem g;
         g.colinfo = 0;                                     // kEpiWarps x kColuFloats floats (u_j)
         g.bars = g.colinfo + kEpiWarps * kColuFloats * 4;  // mbarriers
         g.misc = g.bars + nbars * 8;                       // tmem slot, abort flag
-        g.a_tile = (g.misc + 16 + 1023) & ~1023u;
+        g.cq = g.misc + 16;                                // kChunkRing posted chunk starts (int64)
+        g.a_tile = (g.cq + 8 * kChunkRing + 1023) & ~1023u;
         g.slot_bytes = (uint32_t)(kch * nt) * kChunkBytes;
         g.b_ring = g.a_tile + (uint32_t)kch * kChunkBytes;
         const uint32_t room = kSmemLimit - 1024 - g.b_ring;  // 1024: alignment slack of the block base
         g.nslots = (int)(room / g.slot_bytes);
         if (g.nslots > kMaxSlots) g.nslots = kMaxSlots;
+        if (max_slots >= 2 && g.nslots > max_slots) g.nslots = max_slots;
         g.total = g.b_ring + (uint32_t)g.nslots * g.slot_bytes;
         return g;
     }
@@ -278,14 +290,14 @@ __host__ __device__ constexpr uint32_t gram_idesc_f8(int nt)
 
 // Four-deep register prefetch of the item list, so that the dependent global load of
 // the next item is issued several items ahead of its use.
+// (Item indices are below 2^31: the schedule checks the tile-pair count.)
 struct ItemPrefetch {
     int4 q0, q1, q2, q3;
     const int4* __restrict__ p;
-    unsigned long long end;
-    unsigned stride;
-    __device__ __forceinline__ int4 ld(unsigned long long w) const { return w < end ? p[w] : make_int4(-1, -1, -1, -1); }
-    __device__ __forceinline__ void init(const int4* __restrict__ items, unsigned long long w, unsigned long long e,
-                                         unsigned step = 1)
+    uint32_t end;
+    uint32_t stride;
+    __device__ __forceinline__ int4 ld(uint32_t w) const { return w < end ? p[w] : make_int4(-1, -1, -1, -1); }
+    __device__ __forceinline__ void init(const int4* __restrict__ items, uint32_t w, uint32_t e, uint32_t step = 1)
     {
         p = items;
         end = e;
@@ -296,16 +308,33 @@ struct ItemPrefetch {
         q3 = ld(w + 3 * step);
     }
     // returns item w (the next item of this sequence) and prefetches item w + 4 * stride
-    __device__ __forceinline__ int4 next(unsigned long long w)
+    __device__ __forceinline__ int4 next(uint32_t w)
     {
         const int4 r = q0;
         q0 = q1;
         q1 = q2;
         q2 = q3;
-        q3 = ld(w + 4ull * stride);
+        q3 = ld(w + 4u * stride);
         return r;
     }
 };
+
+// Next chunk posted by the producer for a consumer at ring position (cs, cph): its first
+// item, or -1 when the queue is empty.  Returns false when the wait ran out or the CTA
+// aborts.  Every consumer (the MMA thread, each epilogue warp's lane 0) takes every chunk.
+__device__ __forceinline__ bool take_chunk(uint64_t* cq_full, uint64_t* cq_empty, volatile long long* cqv, int& cs,
+                                           uint32_t& cph, long long& start, volatile int* abort_flag, int* fault,
+                                           int where)
+{
+    if (!mbar_wait_fast(&cq_full[cs], cph, abort_flag, fault, where)) return false;
+    start = cqv[cs];
+    mbar_arrive(&cq_empty[cs]);
+    if (++cs == kChunkRing) {
+        cs = 0;
+        cph ^= 1u;
+    }
+    return true;
+}
 
 // ------------------------------------------------------------------------------------------------
 // the Gram kernel
@@ -331,14 +360,14 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
                 unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
-                const unsigned long long* __restrict__ sched, int* __restrict__ fault)
+                unsigned long long* __restrict__ qhead, int chunk, int max_slots, int* __restrict__ fault)
 {
     constexpr int kAcc = kTmemCols / (kAccCols * NT);  // accumulators in flight
     constexpr uint32_t kIdesc = F8 ? gram_idesc_f8(NT) : gram_idesc(NT);
     constexpr int kChunkElems = F8 ? 2 * kChunkK : kChunkK;  // elements per 128-byte chunk row
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
-    const GramSmem SL = GramSmem::make(KCH, NT);
+    const GramSmem SL = GramSmem::make(KCH, NT, max_slots);
     uint64_t* bars = (uint64_t*)(sm + SL.bars);
     uint64_t* a_full = bars;
     uint64_t* a_empty = bars + 1;
@@ -347,6 +376,9 @@ __global__ void __maxnreg__(kGramMaxRegs)
     uint64_t* tfull = bars + 2 + 2 * kMaxSlots;
     uint64_t* tempty = tfull + kAccBufs;
     uint64_t* drain = tempty + kAccBufs;
+    uint64_t* cq_full = drain + 1;             // chunk ring: posted by the producer
+    uint64_t* cq_empty = cq_full + kChunkRing; // read by the MMA thread and every epilogue warp
+    volatile long long* cqv = (volatile long long*)(sm + SL.cq);  // chunk's first item, -1: queue empty
     // ring slots: one item (all K-chunks of its NT B tiles) per slot
     const int nslots = SL.nslots;
     const uint32_t slot_bytes = SL.slot_bytes;
@@ -371,6 +403,10 @@ __global__ void __maxnreg__(kGramMaxRegs)
             mbar_init(&tempty[b], kGroupWarps * NT);
         }
         mbar_init(drain, 1);
+        for (int k = 0; k < kChunkRing; ++k) {
+            mbar_init(&cq_full[k], 1);
+            mbar_init(&cq_empty[k], 1 + kEpiWarps);
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -379,8 +415,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    const unsigned long long wbeg = min(nitems, sched[blockIdx.x]);
-    const unsigned long long wend = min(nitems, sched[blockIdx.x + 1]);
+    const unsigned long long uchunk = (unsigned long long)chunk;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -392,40 +427,77 @@ __global__ void __maxnreg__(kGramMaxRegs)
             int cur_i = -1;
             uint32_t issued = 0, last_phase = 0;  // per ring slot: loads issued, phase of the last
             bool ok = true;
-            ItemPrefetch pf;
-            pf.init(items, wbeg, wend);
+            ItemPrefetch pf, pfn;  // pfn: the first items of the next chunk, loaded ahead
             int q = 0;
             uint32_t ph = 0;
-            for (unsigned long long w = wbeg; ok && w < wend; ++w) {
-                const int4 it = pf.next(w);
-                if (it.x != cur_i) {
-                    if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
-                    mbar_expect_tx(a_full, kTileBytes);
+            int cs = 0;
+            uint32_t cph = 0;
+            // posts a chunk (its first item, or -1 when the queue is empty) to the consumers
+            auto post = [&](long long v) -> bool {
+                if (!mbar_wait_fast(&cq_empty[cs], cph ^ 1u, abort_flag, fault, 7)) return false;
+                cqv[cs] = v;
+                mbar_arrive(&cq_full[cs]);
+                if (++cs == kChunkRing) {
+                    cs = 0;
+                    cph ^= 1u;
+                }
+                return true;
+            };
+            unsigned long long c0 = atomicAdd(qhead, 1ull) * uchunk;  // this CTA's first chunk
+            bool more = c0 < nitems;
+            ok = post(more ? (long long)c0 : -1ll);
+            bool ahead = false;  // pfn holds the current chunk's items
+            while (ok && more) {
+                const unsigned long long cend = min(nitems, c0 + uchunk);
+                // the next chunk's ticket, in flight while this chunk's loads are issued
+                const unsigned long long tk_next = atomicAdd(qhead, 1ull);
+                unsigned long long n0 = 0;
+                if (ahead) pf = pfn;
+                else pf.init(items, c0, cend);
+                ahead = false;
+                for (unsigned long long w = c0; w < cend; ++w) {
+                    // four items before the end, the next chunk's first items are requested
+                    if (!ahead && w + 4 >= cend) {
+                        n0 = tk_next * uchunk;
+                        if (n0 < nitems) {
+                            pfn.init(items, n0, min(nitems, n0 + uchunk));
+                            ahead = true;
+                        }
+                    }
+                    const int4 it = pf.next(w);
+                    if (it.x != cur_i) {
+                        if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
+                        mbar_expect_tx(a_full, kTileBytes);
 #pragma unroll
-                    for (int kc = 0; kc < KCH; ++kc)
-                        tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkElems, it.x * kTile);
-                    ++aloads;
-                    cur_i = it.x;
-                }
-                if (!mbar_wait_fast(&b_empty[q], ph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
-                const bool second = NT == 2 && it.z >= 0;
-                mbar_expect_tx(&b_full[q], second ? 2 * kTileBytes : kTileBytes);
-                uint8_t* slot = sm + SL.b_ring + q * slot_bytes;
-                // chunk kc of tile t at slot + (kc NT + t) 16 KB: per chunk the NT tiles are
-                // stacked rows of one 128 NT-row operand
+                        for (int kc = 0; kc < KCH; ++kc)
+                            tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkElems, it.x * kTile);
+                        ++aloads;
+                        cur_i = it.x;
+                    }
+                    if (!mbar_wait_fast(&b_empty[q], ph ^ 1u, abort_flag, fault, 2)) { ok = false; break; }
+                    const bool second = NT == 2 && it.z >= 0;
+                    mbar_expect_tx(&b_full[q], second ? 2 * kTileBytes : kTileBytes);
+                    uint8_t* slot = sm + SL.b_ring + q * slot_bytes;
+                    // chunk kc of tile t at slot + (kc NT + t) 16 KB: per chunk the NT tiles are
+                    // stacked rows of one 128 NT-row operand
 #pragma unroll
-                for (int kc = 0; kc < KCH; ++kc) {
-                    tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems, it.y * kTile);
-                    if (second)
-                        tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems,
-                                    it.z * kTile);
+                    for (int kc = 0; kc < KCH; ++kc) {
+                        tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems, it.y * kTile);
+                        if (second)
+                            tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems,
+                                        it.z * kTile);
+                    }
+                    issued |= 1u << q;
+                    last_phase = (last_phase & ~(1u << q)) | (ph << q);
+                    if (++q == nslots) {
+                        q = 0;
+                        ph ^= 1u;
+                    }
                 }
-                issued |= 1u << q;
-                last_phase = (last_phase & ~(1u << q)) | (ph << q);
-                if (++q == nslots) {
-                    q = 0;
-                    ph ^= 1u;
-                }
+                if (!ok) break;
+                c0 = tk_next * uchunk;
+                more = c0 < nitems;
+                ok = post(more ? (long long)c0 : -1ll);
             }
             if (!ok) {
                 // drain: the copies in flight must land before the CTA exits
@@ -456,8 +528,15 @@ __global__ void __maxnreg__(kGramMaxRegs)
             const uint64_t slot_step = (uint64_t)(slot_bytes >> 4);  // descriptor address units
             uint64_t bdesc_q = bdesc_ring;
             ItemPrefetch pf;
-            pf.init(items, wbeg, wend);
-            for (unsigned long long w = wbeg; ok && w < wend; ++w) {
+            int cs = 0;
+            uint32_t cph = 0;
+            long long st = -1;
+            ok = take_chunk(cq_full, cq_empty, cqv, cs, cph, st, abort_flag, fault, 8);
+            while (ok && st >= 0) {
+            const unsigned long long c0 = (unsigned long long)st, cend = min(nitems, c0 + uchunk);
+            long long nst = -1;  // the next chunk, taken at this chunk's last item
+            pf.init(items, c0, cend);
+            for (unsigned long long w = c0; w < cend; ++w) {
                 const int4 it = pf.next(w);
                 if (it.x != cur_i) {
                     if (!mbar_wait_fast(a_full, aidx & 1u, abort_flag, fault, 3)) { ok = false; break; }
@@ -484,8 +563,19 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 any = true;
                 umma_commit(&b_empty[q]);
                 umma_commit(&tfull[b]);
-                // release the A tile after its last item's MMAs
-                if (pf.q0.x != cur_i) umma_commit(a_empty);  // pf.q0 is item w + 1 (or -1 past the end)
+                // release the A tile after its last item's MMAs; the next item is pf.q0 inside the
+                // chunk, else the first item of the next chunk (-1 at the end of the queue)
+                int next_row;
+                if (w + 1 < cend) {
+                    next_row = pf.q0.x;
+                } else {
+                    if (!take_chunk(cq_full, cq_empty, cqv, cs, cph, nst, abort_flag, fault, 9)) {
+                        ok = false;
+                        nst = -1;
+                    }
+                    next_row = nst >= 0 ? items[nst].x : -1;
+                }
+                if (next_row != cur_i) umma_commit(a_empty);
                 if (++q == nslots) {
                     q = 0;
                     ph ^= 1u;
@@ -497,6 +587,8 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     b = 0;
                     tph ^= 1u;
                 }
+            }
+            st = nst;
             }
             if (!ok && any) {
                 // wait (bounded) for the MMAs already issued before tensor memory is freed
@@ -521,35 +613,64 @@ __global__ void __maxnreg__(kGramMaxRegs)
         const int cg = (ew % kGroupWarps) >> 2;        // column group: columns [kEpiCols cg, +kEpiCols)
         const int half = NT == 2 ? grp : 0;
         const unsigned ustride = NT == 2 ? 1u : (unsigned)kEpiGroups;
-        const unsigned long long ubeg = wbeg + (NT == 2 ? 0 : grp);
+        const uint32_t goff = NT == 2 ? 0u : (uint32_t)grp;  // first unit in a chunk
         float* colu = (float*)(sm + SL.colinfo) + ew * kColuFloats;
         const int r = sub * 32 + lane;
-        ItemPrefetch pf;
-        pf.init(items, ubeg, wend, ustride);
-        // row / column data of the current unit, loaded one unit ahead; of an item only its
-        // row tile and this group's column tile are kept (it_i, it_j)
-        int it_i, it_j;
-        {
-            const int4 it = pf.next(ubeg);
-            it_i = it.x;
-            it_j = half ? it.z : it.y;
-        }
-        float2 uc = make_float2(0.f, 0.f);
-        float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 tj = make_float2(0.f, 0.f);
-        if (ubeg < wend && it_j >= 0) {
-            if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
-            ri = rowinfo[(int64_t)it_i * kTile + r];
-            tj = tileinfo[it_j];
-        }
         // Fragment layout (tcgen05.ld.16x256b): thread (rq, q4) = (lane / 4, lane % 4) holds
         // rows rq + 8 k (k = 0..3) of this sub-partition and columns 8 m + 2 q4 + e
         // (m = 0..7, e = 0..1) of the warp's 64: 16 column terms u_j per thread and item
         // (with a 32x32b load every thread would need all 64).
         const int rq = lane >> 2, q4 = lane & 3;
         const int n32 = (int)n;
-        uint32_t local = (uint32_t)(ubeg - wbeg);  // item index within the CTA's range
-        for (unsigned long long w = ubeg; w < wend; w += ustride, local += ustride) {
+        int cs = 0;
+        uint32_t cph = 0;
+        bool alive = true;
+        // The queue's chunks as this warp sees them: (c0, cend) the current chunk, base the
+        // CTA-sequence index of its item c0.  take_next() moves to the next chunk in which
+        // this warp has a unit and returns false at the end of the queue (or when the wait
+        // ran out); it runs one unit ahead, while the current unit waits for its accumulator.
+        const uint32_t nit = (uint32_t)nitems, uch = (uint32_t)chunk;
+        uint32_t c0 = 0, cend = 0;
+        uint32_t base = 0;
+        auto take_next = [&]() -> bool {
+            for (;;) {
+                long long st = -1;
+                bool got = true;
+                if (lane == 0) got = take_chunk(cq_full, cq_empty, cqv, cs, cph, st, abort_flag, fault, 10);
+                got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+                st = __shfl_sync(0xffffffffu, st, 0);
+                if (!got) alive = false;
+                if (!got || st < 0) return false;
+                base += cend - c0;
+                c0 = (uint32_t)st;
+                cend = min(nit, c0 + uch);
+                if (c0 + (uint32_t)goff < cend) return true;  // chunks other than the last have even sizes
+            }
+        };
+        // row / column data of the current unit, loaded one unit ahead; of an item only its
+        // row tile and this group's column tile are kept (it_i, it_j)
+        int it_i = -1, it_j = -1;
+        float2 uc = make_float2(0.f, 0.f);
+        float4 ri = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 tj = make_float2(0.f, 0.f);
+        uint32_t w = 0;
+        uint32_t local = 0;  // item index in the CTA's sequence
+        ItemPrefetch pf;
+        bool have = take_next();
+        if (have) {
+            w = c0 + goff;
+            local = base + (uint32_t)goff;
+            pf.init(items, w, cend, ustride);
+            const int4 it = pf.next(w);
+            it_i = it.x;
+            it_j = half ? it.z : it.y;
+            if (it_j >= 0) {
+                if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
+                ri = rowinfo[(int64_t)it_i * kTile + r];
+                tj = tileinfo[it_j];
+            }
+        }
+        while (have) {
             const int b = (int)(local % (uint32_t)kAcc);
             const uint32_t tph = (local / (uint32_t)kAcc) & 1u;
             const int jt = it_j;  // this unit's column tile (-1: none)
@@ -568,12 +689,27 @@ __global__ void __maxnreg__(kGramMaxRegs)
 #pragma unroll
                 for (int k = 0; k < 4; ++k) Wk[k] = __shfl_sync(0xffffffffu, Wi, rq + 8 * k);
             }
-            // issue the next unit's loads now; they complete while this one is tested
+            // the next unit (in this chunk, or the first of the next one) and its loads, issued
+            // now: they complete while this unit is tested
+            uint32_t wn = w + ustride;
+            uint32_t ln = local + ustride;
+            bool nhave = true;
             {
-                const int4 itn = pf.next(w + ustride);
-                it_i = itn.x;
-                it_j = half ? itn.z : itn.y;
-                if (w + ustride < wend && it_j >= 0) {
+                int4 itn;
+                if (wn < cend) {
+                    itn = pf.next(wn);
+                } else {
+                    nhave = take_next();
+                    if (nhave) {
+                        wn = c0 + goff;
+                        ln = base + (uint32_t)goff;
+                        pf.init(items, wn, cend, ustride);
+                        itn = pf.next(wn);
+                    }
+                }
+                it_i = nhave ? itn.x : -1;
+                it_j = nhave ? (half ? itn.z : itn.y) : -1;
+                if (nhave && it_j >= 0) {
                     if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
                     ri = rowinfo[(int64_t)it_i * kTile + r];
                     tj = tileinfo[it_j];
@@ -584,7 +720,10 @@ __global__ void __maxnreg__(kGramMaxRegs)
             if (!__all_sync(0xffffffffu, mbar_try_wait(&tfull[b], tph))) {
                 bool ready = (lane == 0) ? mbar_wait(&tfull[b], tph, abort_flag, fault, 6) : false;
                 ready = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
-                if (!ready) break;
+                if (!ready) {
+                    alive = false;
+                    break;
+                }
                 while (!mbar_try_wait(&tfull[b], tph)) {
                 }
             }
@@ -594,8 +733,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&tempty[b]);
-                continue;
-            }
+            } else {
             const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) +
                                    (uint32_t)(b * kAccCols * NT + half * kAccCols + cg * kEpiCols);
             // this thread's column terms: u2[m] = u_j of columns 8 m + 2 q4 + {0, 1}
@@ -699,8 +837,13 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     }
                 }
             }
+            }
             __syncwarp();
+            w = wn;
+            local = ln;
+            have = nhave;
         }
+        (void)alive;
     }
 
     tc_fence_before();
@@ -1171,7 +1314,7 @@ static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, co
                           const CUtensorMap& tmb, const int4* items,
                           unsigned long long nitems, const float4* rowinfo, const float* ucol, const float2* tileinfo,
                           int64_t n, float eps_p, float kappa, uint2* cand, unsigned long long* cnt,
-                          unsigned long long ccap, const unsigned long long* sched, int* fault)
+                          unsigned long long ccap, unsigned long long* qhead, int chunk, int max_slots, int* fault)
 {
     if (!launch) {
         RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1179,7 +1322,8 @@ static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, co
         return;
     }
     k_gram_bf16<KCH, NT, FOLD, F8><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
-                                                                eps_p, kappa, cand, cnt, ccap, sched, fault);
+                                                                eps_p, kappa, cand, cnt, ccap, qhead, chunk,
+                                                                max_slots, fault);
 }
 
 // Sets the shared-memory size (launch = false) or launches the instance for (kch, nt, fold).
@@ -1207,10 +1351,99 @@ static void gram_dispatch(bool fold, bool f8, int kch, int nt, Args... args)
     else gram_dispatch_fold<false>(kch, nt, args...);
 }
 
-int gram_item_tiles(int d)
+GramTune gram_tune(rnng_ctx* c, int kind, int dp, int64_t tile_pairs)
 {
+    GramTune t;
+    t.kind = kind;
+    t.dp = dp;
     // two column tiles per item (N = 256 MMAs) while two B slots of them fit next to A
-    return ceil_div(d, kChunkK) <= 2 ? 2 : 1;
+    t.nt = (kind == 0 && dp <= 2 * kChunkK) ? 2 : 1;
+    t.chunk = 64;
+    t.slots = 0;
+    const GramTune* best = nullptr;
+    for (const GramTune& r : c->gram_table)
+        if (r.kind == kind && r.dp == dp && r.min_pairs <= tile_pairs && (!best || r.min_pairs >= best->min_pairs))
+            best = &r;
+    const GramTune* src[2] = {best, &c->gram_force};
+    for (const GramTune* r : src) {
+        if (!r) continue;
+        if (r->nt > 0) t.nt = r->nt;
+        if (r->chunk > 0) t.chunk = r->chunk;
+        if (r->slots > 0) t.slots = r->slots;
+    }
+    // compiled forms: two column tiles only for BF16 operands of at most two K-chunks
+    if (kind != 0 || dp > 2 * kChunkK || t.nt != 2) t.nt = 1;
+    t.chunk = std::max(1, std::min(t.chunk, 1 << 20));
+    // with one column tile the two epilogue groups take alternate items of a chunk: even sizes
+    if (t.nt == 1) t.chunk = (t.chunk + 1) & ~1;
+    if (t.slots == 1) t.slots = 2;
+    return t;
+}
+
+namespace {
+
+// The integer after "key": in a JSON object's text (nullopt-like: returns false if absent).
+bool json_int(const std::string& obj, const char* key, long long* out)
+{
+    const std::string k = std::string("\"") + key + "\"";
+    size_t p = obj.find(k);
+    if (p == std::string::npos) return false;
+    p = obj.find(':', p + k.size());
+    if (p == std::string::npos) return false;
+    ++p;
+    while (p < obj.size() && (obj[p] == ' ' || obj[p] == '\t' || obj[p] == '\n' || obj[p] == '\r')) ++p;
+    char* end = nullptr;
+    const long long v = std::strtoll(obj.c_str() + p, &end, 10);
+    if (end == obj.c_str() + p) return false;
+    *out = v;
+    return true;
+}
+
+std::string library_dir()
+{
+    Dl_info info;
+    if (dladdr((const void*)&library_dir, &info) && info.dli_fname) {
+        std::string f = info.dli_fname;
+        const size_t s = f.rfind('/');
+        return s == std::string::npos ? std::string(".") : f.substr(0, s);
+    }
+    return ".";
+}
+
+}  // namespace
+
+void load_gram_table(rnng_ctx* c)
+{
+    c->gram_table.clear();
+    const char* env = std::getenv("RNNG_GRAM_TUNING");
+    // the library sits in rnng_gb300/_build/, the table in rnng_gb300/
+    const std::string path = env && *env ? std::string(env) : library_dir() + "/../gram_tuning.json";
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return;
+    std::string text;
+    char buf[4096];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
+    std::fclose(f);
+    // {"rows": [{"kind": "bf16" | "f8", "dp": .., "min_pairs": .., "nt": .., "chunk": .., "slots": ..}, ...]}
+    size_t p = text.find("\"rows\"");
+    if (p == std::string::npos) return;
+    while ((p = text.find('{', p)) != std::string::npos) {
+        const size_t e = text.find('}', p);
+        if (e == std::string::npos) break;
+        const std::string obj = text.substr(p, e - p + 1);
+        p = e + 1;
+        long long dp = 0, mp = 0, nt = 0, ch = 0, sl = 0;
+        if (!json_int(obj, "dp", &dp)) continue;
+        GramTune r;
+        r.kind = obj.find("\"f8\"") != std::string::npos ? 1 : 0;
+        r.dp = (int)dp;
+        if (json_int(obj, "min_pairs", &mp)) r.min_pairs = mp;
+        if (json_int(obj, "nt", &nt)) r.nt = (int)nt;
+        if (json_int(obj, "chunk", &ch)) r.chunk = (int)ch;
+        if (json_int(obj, "slots", &sl)) r.slots = (int)sl;
+        c->gram_table.push_back(r);
+    }
 }
 
 // Candidates of the scheduled items of L by the tensor-core kernel, with the candidate
@@ -1223,21 +1456,29 @@ static unsigned long long gram_candidates(rnng_ctx* c, const Layout& L, const CU
 {
     cudaStream_t s = c->stream;
     unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
-    const GramSmem layout = GramSmem::make(kchunks, nt);
+    const GramSmem layout = GramSmem::make(kchunks, nt, L.gram_slots);
     RNNG_REQUIRE(layout.nslots >= 2, RNNG_ERR_UNSUPPORTED, "BF16 operand tiles too large for shared memory");
     const size_t smem = layout.total + 1024;
+    const int chunk = std::max(1, L.gram_chunk);
+    unsigned long long* qhead = c->counters.as<unsigned long long>() + kSlotQueue;
     gram_dispatch(fold, f8, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
-                  L.n, eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, L.sched, c->fault_word);
-    const int grid = L.sched_G;
-    RNNG_REQUIRE(grid >= 1, RNNG_ERR_INVALID, "tile pairs were not scheduled");
+                  L.n, eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, qhead, chunk, L.gram_slots, c->fault_word);
+    // one CTA per SM, fewer when there are fewer chunks
+    const int grid = (int)std::max<unsigned long long>(
+        1, std::min<unsigned long long>((L.num_items + chunk - 1) / chunk, (unsigned long long)c->num_sms));
+    c->stats.gram_nt = nt;
+    c->stats.gram_chunk = chunk;
+    c->stats.gram_slots = layout.nslots;
     const float kappa = 1.0f / (1 << 20);  // relative slack for the fp32 evaluation of the test
     unsigned long long got = 0;
     for (int attempt = 0;; ++attempt) {
         c->cand.reserve(sizeof(uint2) * ccap);
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+        RNNG_CUDA(cudaMemsetAsync(qhead, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
         gram_dispatch(fold, f8, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol,
-                      tileinfo, L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, L.sched, c->fault_word);
+                      tileinfo, L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, qhead, chunk, L.gram_slots,
+                      c->fault_word);
         ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));

@@ -85,6 +85,18 @@ def test_integer_descriptors_30k(ctx, orc, mode):
     assert same(ctx.eps_graph_l2(x, r, mode=mode), orc.eps_graph_l2(x, r))
 
 
+def test_small_dimensions_take_fp32_tiles(ctx, orc):
+    """BF16 mode evaluates tiles of fewer than 16 dimensions on the CUDA cores (no Gram
+    kernel time), from 16 on with the tensor-core Gram form; both give RNNG's edges."""
+    from rnng_gb300 import synth
+    for d, gram in ((8, False), (15, False), (16, True)):
+        x = synth.l2_mixture(n=3000, d=d, seed=d)
+        r = np.float32(1.1 * np.sqrt(d))
+        got = ctx.eps_graph_l2(x, r, mode="bf16")
+        assert (ctx.stats()["ms_gram"] > 0) == gram
+        assert same(got, orc.eps_graph_l2(x, r)) and got[0].size > 0
+
+
 def test_modes_agree_and_fp64_error(ctx):
     from rnng_gb300 import synth
     x = synth.zipf_mixture(n=40000, d=32, k=256, seed=21)
@@ -117,7 +129,7 @@ def test_both_pruning_paths_exact(ctx, orc, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("d", [8, 100, 300])
+@pytest.mark.parametrize("d", [8, 24, 100, 300])
 def test_nonfinite_rows(ctx, orc, mode, d):
     """Rows with a NaN or infinite coordinate get no edges and leave every other edge in
     place (RNNG's dist <= radius is false for them); NaN, +inf and -inf, single
@@ -200,11 +212,40 @@ def test_power_of_two_scales(ctx, orc, mode, e):
     """The same point set scaled by 2^e (exact in float32): RNNG's L2 of the scaled
     points, subnormal squares at the small end included, decides the edges."""
     rng = np.random.default_rng(88)
-    centres = rng.uniform(-4, 4, size=(6, 12))
-    base = (centres[rng.integers(0, 6, 2500)] + rng.normal(size=(2500, 12))).astype(np.float32)
+    centres = rng.uniform(-4, 4, size=(6, 16))
+    base = (centres[rng.integers(0, 6, 2500)] + rng.normal(size=(2500, 16))).astype(np.float32)
     s = np.float32(2.0 ** e)
     x = (base * s).astype(np.float32)
-    r = np.float32(np.float32(2.6) * s)
+    r = np.float32(np.float32(3.6) * s)
     want = orc.eps_graph_l2(x, r)
     assert want[0].size > 3000
     assert same(ctx.eps_graph_l2(x, r, mode=mode), want)
+
+
+def test_gram_tuning_table_and_override(ctx, orc):
+    """The Gram kernel's work-queue chunk, column tiles per item and B slots come from the
+    committed tuning table (rnng_gb300/gram_tuning.json) and can be forced per context;
+    every setting gives RNNG's edges."""
+    import json
+    import os
+
+    from rnng_gb300 import synth
+    table = json.load(open(os.path.join(os.path.dirname(synth.__file__), "gram_tuning.json")))["rows"]
+    row = min((r for r in table if r["kind"] == "bf16" and r["dp"] == 64), key=lambda r: r["min_pairs"])
+    x = synth.zipf_mixture(n=20000, d=32, k=64, seed=41)
+    r = np.float32(4.5)
+    want = orc.eps_graph_l2(x, r)
+    got = ctx.eps_graph_l2(x, r, mode="bf16")
+    st = ctx.stats()
+    assert st["tile_pairs"] < max(t["min_pairs"] for t in table if t["dp"] == 64) or len(table) == 1
+    assert (st["gram_nt"], st["gram_chunk"]) == (row["nt"], row["chunk"])
+    assert same(got, want)
+    for nt, chunk, slots in ((2, 1, 2), (1, 2, 3), (2, 7, 0), (1, 5, 2)):
+        ctx.set_gram_tuning(nt, chunk, slots)
+        got = ctx.eps_graph_l2(x, r, mode="bf16")
+        st = ctx.stats()
+        assert st["gram_nt"] == nt and st["gram_chunk"] == (chunk + (chunk & 1 if nt == 1 else 0))
+        assert same(got, want)
+    ctx.set_gram_tuning(0, 0, 0)
+    ctx.eps_graph_l2(x, r, mode="bf16")
+    assert (ctx.stats()["gram_nt"], ctx.stats()["gram_chunk"]) == (row["nt"], row["chunk"])

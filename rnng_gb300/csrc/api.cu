@@ -219,7 +219,8 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->aux0, &c->aux1, &c->aux2, &c->aux3, &c->aux4, &c->aux5, &c->aux6, &c->aux7, &c->sched,
                           &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
                           &c->items, &c->items_tmp, &c->sched_tmp, &c->sym, &c->shift_buf, &c->ball_b16,
-                          &c->ball_info, &c->lm_b16, &c->xb_sortedB, &c->fin_x, &c->fin_idx};
+                          &c->ball_info, &c->sball_b16, &c->sball_info, &c->lm_b16, &c->xb_sortedB, &c->fin_x,
+                          &c->fin_idx};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

@@ -191,18 +191,19 @@ __device__ __forceinline__ void cover_argmax(CoverState& st, float v, int i)
 
 // Up to K groups of the n items; centres into cen[K][d] (global, owned by the block),
 // radii into rad[K] (-1: no group).  `cbuf` is d floats of shared memory for the centroid.
-__device__ void cover_groups(CoverState& st, const float* __restrict__ src, const float* __restrict__ irad, int n,
-                             int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ cen,
+__device__ void cover_groups(CoverState& st, const float* __restrict__ src, int ld, const float* __restrict__ irad,
+                             int n, int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ cen,
                              float* __restrict__ rad)
 {
+    // item r is src[r ld .. r ld + d)
     const int t = threadIdx.x;
     const bool mine = t < n;
-    const float* xr = src + (int64_t)(mine ? t : 0) * d;
+    const float* xr = src + (int64_t)(mine ? t : 0) * ld;
     const float ir = (mine && irad) ? irad[t] : 0.f;
     // centroid of all items
     for (int k = t; k < d; k += blockDim.x) {
         float a = 0.f;
-        for (int r = 0; r < n; ++r) a += src[(int64_t)r * d + k];
+        for (int r = 0; r < n; ++r) a += src[(int64_t)r * ld + k];
         cbuf[k] = n > 0 ? a / (float)n : 0.f;
     }
     if (t < kCoverMaxBalls) {
@@ -218,7 +219,7 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, cons
         const int j = st.pick;
         if (ng > 0 && !(st.pick_v > 0.f)) break;  // every item coincides with a centre
         if (mine) {
-            const float dj = row_dist(xr, src + (int64_t)j * d, d) + ir;
+            const float dj = row_dist(xr, src + (int64_t)j * ld, d) + ir;
             if (ng == 0 || dj < dm) {
                 dm = dj;
                 lab = ng;
@@ -235,7 +236,7 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, cons
             int c = 0;
             for (int r = 0; r < n; ++r)
                 if (st.label[r] == g) {
-                    a += src[(int64_t)r * d + k];
+                    a += src[(int64_t)r * ld + k];
                     ++c;
                 }
             cen[(int64_t)g * d + k] = c ? a / (float)c : 0.f;
@@ -253,9 +254,10 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, cons
 }
 
 // One block per tile.  Output: centres [T][kTileBalls][d], radii [T][kTileBalls] (-1 =
-// unused).  With staged = true the tile's rows are first copied to shared memory, which
-// every pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), plus
-// kTile * d floats when staged.
+// unused).  With staged = true the tile's rows are first copied to shared memory (rows
+// d + 1 floats apart, so that the threads' row walks hit distinct banks), which every
+// pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), plus
+// kTile (d + 1) floats when staged.
 __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d,
                                                               float grow, bool staged, float* __restrict__ cen,
                                                               float* __restrict__ rad)
@@ -268,19 +270,28 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
     const int64_t r0 = t * kTile;
     const int nitems = (int)min((int64_t)kTile, n - r0);
     const float* src = Xs + r0 * d;
+    int ld = d;
     if (staged) {
         const int total = nitems * d;
         if ((d & 3) == 0) {
             const float4* s4 = reinterpret_cast<const float4*>(src);
-            float4* t4 = reinterpret_cast<float4*>(tile_rows);
-            for (int i = threadIdx.x; i < total / 4; i += blockDim.x) t4[i] = __ldg(s4 + i);
+            for (int i = threadIdx.x; i < total / 4; i += blockDim.x) {
+                const float4 v = __ldg(s4 + i);
+                const int r = (4 * i) / d, k = (4 * i) % d;  // d % 4 == 0: the four stay in row r
+                float* dst = tile_rows + r * (d + 1) + k;
+                dst[0] = v.x;
+                dst[1] = v.y;
+                dst[2] = v.z;
+                dst[3] = v.w;
+            }
         } else {
-            for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[i] = __ldg(src + i);
+            for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[(i / d) * (d + 1) + i % d] = __ldg(src + i);
         }
         __syncthreads();
         src = tile_rows;
+        ld = d + 1;
     }
-    cover_groups(st, src, nullptr, nitems, d, kTileBalls, grow, cbuf, cen + t * kTileBalls * d,
+    cover_groups(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, cen + t * kTileBalls * d,
                  rad + t * kTileBalls);
 }
 
@@ -316,7 +327,7 @@ __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __re
         for (int j = threadIdx.x; j < d; j += blockDim.x)
             items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
     __syncthreads();
-    cover_groups(st, items, irad, m, d, kSuperBalls, grow, dsm, scen + s * kSuperBalls * d, srad + s * kSuperBalls);
+    cover_groups(st, items, d, irad, m, d, kSuperBalls, grow, dsm, scen + s * kSuperBalls * d, srad + s * kSuperBalls);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -372,6 +383,104 @@ __global__ void k_bitmap_pairs(const uint32_t* __restrict__ bitmap, int64_t S, i
             if (pos < cap) out[pos] = make_int2((int)(bit / S), (int)(bit % S));
             ++pos;
         }
+    }
+}
+
+// Level 1 on the tensor cores (d <= 256): the same BF16 ball test as k_tile_close_mma
+// (below) over all pairs of super balls.  Block pairs (RB <= CB) of four super-tiles
+// (64 balls) each, taken as contiguous ranges of the row-major upper triangle per CUDA
+// block; warp w takes the 16 balls of row super-tile 4 RB + w against the 64 of the
+// column block, keeps the row block's A fragments in registers while RB lasts, and marks
+// super-tile pair (I, J), I <= J, in the S x S bitmap when any of its ball pairs passes.
+template <int KP>
+__global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict__ cb, const float4* __restrict__ binfo,
+                                                         int64_t S, float eps_p, float kappa,
+                                                         uint32_t* __restrict__ bitmap)
+{
+    constexpr int rowq = 4 * KP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int64_t nR = (S + 3) / 4;
+    const unsigned long long total = (unsigned long long)nR * (nR + 1) / 2;
+    const unsigned long long per = (total + gridDim.x - 1) / gridDim.x;
+    const unsigned long long p0 = (unsigned long long)blockIdx.x * per, p1 = min(total, p0 + per);
+    if (p0 >= p1) return;
+    // (RB, CB) of p0: row RB holds nR - RB block pairs
+    int64_t RB = 0;
+    unsigned long long first = 0;  // index of (RB, RB)
+    {
+        const double a = 2.0 * (double)nR + 1.0;
+        RB = (int64_t)((a - sqrt(a * a - 8.0 * (double)p0)) * 0.5);
+        if (RB < 0) RB = 0;
+        if (RB >= nR) RB = nR - 1;
+        auto row_first = [&](int64_t r) { return (unsigned long long)(r * nR - r * (r - 1) / 2); };
+        while (RB > 0 && row_first(RB) > p0) --RB;
+        while (RB + 1 < nR && row_first(RB + 1) <= p0) ++RB;
+        first = row_first(RB);
+    }
+    int64_t CB = RB + (int64_t)(p0 - first);
+    int64_t cur = -1;
+    uint4 a0[KP], a1[KP];
+    float4 x0 = make_float4(0.f, 0.f, 0.f, -1.f), x1 = x0;
+    for (unsigned long long p = p0; p < p1; ++p) {
+        if (CB >= nR) {
+            ++RB;
+            CB = RB;
+        }
+        const int64_t ra = RB * 64 + 16 * warp, rbb = CB * 64;
+        if (RB != cur) {
+            const uint4* pa = cb + (ra + g) * rowq + t;
+#pragma unroll
+            for (int kp = 0; kp < KP; ++kp) {
+                a0[kp] = pa[4 * kp];
+                a1[kp] = pa[8 * rowq + 4 * kp];
+            }
+            x0 = binfo[ra + g];
+            x1 = binfo[ra + 8 + g];
+            cur = RB;
+        }
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+        const uint4* pb = cb + (rbb + g) * rowq + t;
+#pragma unroll
+        for (int kp = 0; kp < KP; ++kp) {
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint4 b = pb[(8 * nt) * rowq + 4 * kp];
+                mma_bf16_16816(acc[nt], a0[kp].x, a1[kp].x, a0[kp].y, a1[kp].y, b.x, b.y);
+                mma_bf16_16816(acc[nt], a0[kp].z, a1[kp].z, a0[kp].w, a1[kp].w, b.z, b.w);
+            }
+        }
+        // acc[nt][2h + e]: row ball 8 h + g of super-tile 4 RB + warp, column ball 8 nt + 2 t + e
+        // of the column block: super-tile 4 CB + nt / 2
+        uint32_t msk = 0;  // bit c: column super-tile 4 CB + c
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const float4 y = binfo[rbb + 8 * nt + 2 * t + e];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float4 x = h ? x1 : x0;
+                    const float D = fmaf(-2.f, acc[nt][2 * h + e], x.x + y.x);
+                    const float E = eps_p + x.w + y.w + x.y + y.y;
+                    const float R = fmaf(E, E, x.z + y.z);
+                    const bool keep = x.w >= 0.f && y.w >= 0.f && D <= R + kappa * (x.x + y.x + R);
+                    msk |= (keep ? 1u : 0u) << (nt >> 1);
+                }
+            }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) msk |= __shfl_xor_sync(0xffffffffu, msk, o);
+        if (lane < 4 && ((msk >> lane) & 1u)) {
+            const int64_t I = 4 * RB + warp, J = 4 * CB + lane;
+            if (I < S && J < S && I <= J) {
+                const int64_t bit = I * S + J;
+                atomicOr(&bitmap[bit >> 5], 1u << (bit & 31));
+            }
+        }
+        ++CB;
     }
 }
 
@@ -691,7 +800,7 @@ void build_covers(rnng_ctx* c, Layout& L)
     // tiles staged in shared memory up to 128 dimensions (64 KB; larger tiles read through L1)
     const bool staged = L.d <= 128;
     const size_t csm = sizeof(float) * (size_t)((L.d + 3) & ~3);
-    const size_t tsm = csm + (staged ? sizeof(float) * kTile * (size_t)L.d : 0);
+    const size_t tsm = csm + (staged ? sizeof(float) * kTile * (size_t)(L.d + 1) : 0);
     RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
     k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, c->tile_lo.as<float>(),
@@ -709,15 +818,55 @@ void prune_covers(rnng_ctx* c, Layout& L)
     unsigned long long* cnt = c->counters.as<unsigned long long>();
     const float eps_p = widened_radius(L.radius, L.d);
     const float shrink = 1.f - L.relerr;
+    // Tensor-core ball Gram blocks (BF16 ball centres with their error terms) unless those
+    // terms would widen the ball test by more than kMaxWiden on average: data whose extent
+    // is large against eps (then the FP32 kernels prune more).
+    constexpr float kMaxWiden = 0.05f;
+    const bool b16 = bf16_supported(L.d);
+    const int dp = (int)ceil_div(L.d, 64) * 64;
+    bool tc = b16, tcs = b16;
+    const int64_t nsb_pad = ceil_div(L.S, 4) * 64;  // super balls, padded to blocks of four super-tiles
+    if (b16) {
+        const int64_t nb = L.T * kTileBalls, nb_pad = L.S * kSB;
+        c->ball_b16.reserve(sizeof(__nv_bfloat16) * (size_t)nb_pad * dp);
+        c->ball_info.reserve(sizeof(float4) * (size_t)nb_pad);
+        const float widen = prepare_ball_bf16(c, L, c->tile_lo.as<float>(), c->tile_hi.as<float>(), nb, nb_pad, eps_p,
+                                              c->ball_b16.as<__nv_bfloat16>(), c->ball_info.as<float4>());
+        tc = widen <= kMaxWiden;
+        c->stats.prune_widen = widen;
+        c->sball_b16.reserve(sizeof(__nv_bfloat16) * (size_t)nsb_pad * dp);
+        c->sball_info.reserve(sizeof(float4) * (size_t)nsb_pad);
+        const float swiden = prepare_ball_bf16(c, L, c->super_lo.as<float>(), c->super_hi.as<float>(),
+                                               L.S * kSuperBalls, nsb_pad, eps_p, c->sball_b16.as<__nv_bfloat16>(),
+                                               c->sball_info.as<float4>());
+        tcs = swiden <= kMaxWiden;
+    }
+    c->stats.prune_tensor = tc ? 1 : 0;
     // level 1: bitmap of close super-tile pairs
     const int64_t NB = L.S * kSuperBalls;
     const int64_t words = (L.S * L.S + 31) / 32;
     c->aux6.reserve(sizeof(uint32_t) * (size_t)words);
     uint32_t* bitmap = c->aux6.as<uint32_t>();
     RNNG_CUDA(cudaMemsetAsync(bitmap, 0, sizeof(uint32_t) * (size_t)words, s));
-    dim3 g1((unsigned)ceil_div(NB, kDRows), (unsigned)ceil_div(NB, kDCols));
-    k_super_close<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), NB, L.d, eps_p, shrink, bitmap,
-                                     L.S); ++c->launches;
+    if (tcs) {
+        const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
+        const int64_t nR = ceil_div(L.S, 4);
+        const unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nR * (nR + 1) / 2, (int64_t)c->num_sms * 16));
+        auto launch = [&](auto kern) {
+            kern<<<sgrid, 128, 0, s>>>(c->sball_b16.as<uint4>(), c->sball_info.as<float4>(), L.S, eps_p, kappa, bitmap);
+        };
+        switch (dp / 32) {
+            case 2: launch(k_super_close_mma<2>); break;
+            case 4: launch(k_super_close_mma<4>); break;
+            case 6: launch(k_super_close_mma<6>); break;
+            default: launch(k_super_close_mma<8>); break;
+        }
+        ++c->launches;
+    } else {
+        dim3 g1((unsigned)ceil_div(NB, kDRows), (unsigned)ceil_div(NB, kDCols));
+        k_super_close<<<g1, 256, 0, s>>>(c->super_lo.as<float>(), c->super_hi.as<float>(), NB, L.d, eps_p, shrink,
+                                         bitmap, L.S); ++c->launches;
+    }
     const unsigned bgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(words, 256), (int64_t)c->num_sms * 8));
     if ((unsigned long long)L.S * (L.S + 1) / 2 < (1ull << 31)) {
         // row-major pair list: per-word counts, a scan, then each word's pairs at its offset
@@ -757,22 +906,6 @@ void prune_covers(rnng_ctx* c, Layout& L)
     RNNG_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(unsigned long long), s));
     const unsigned grid = (unsigned)std::max<unsigned long long>(
         1, std::min<unsigned long long>((L.super_pairs + kSPB - 1) / kSPB, (unsigned long long)c->num_sms * 8));
-    // Tensor-core ball Gram blocks (BF16 ball centres padded to S super-tiles of kSB rows)
-    // unless their error terms would widen the ball test by more than kMaxWiden on
-    // average: data whose extent is large against eps (then the FP32 kernel prunes more).
-    constexpr float kMaxWiden = 0.05f;
-    bool tc = bf16_supported(L.d);
-    const int dp = (int)ceil_div(L.d, 64) * 64;
-    if (tc) {
-        const int64_t nb = L.T * kTileBalls, nb_pad = L.S * kSB;
-        c->ball_b16.reserve(sizeof(__nv_bfloat16) * (size_t)nb_pad * dp);
-        c->ball_info.reserve(sizeof(float4) * (size_t)nb_pad);
-        const float widen = prepare_ball_bf16(c, L, c->tile_lo.as<float>(), c->tile_hi.as<float>(), nb, nb_pad, eps_p,
-                                              c->ball_b16.as<__nv_bfloat16>(), c->ball_info.as<float4>());
-        tc = widen <= kMaxWiden;
-        c->stats.prune_widen = widen;
-    }
-    c->stats.prune_tensor = tc ? 1 : 0;
     if (tc) {
         const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
         const unsigned wgrid = (unsigned)std::max<unsigned long long>(

@@ -100,7 +100,8 @@ struct rnng_ctx {
     rnng::DevBuf x_in, ids_in, x_sorted, xb_sorted, norms, perm, keys, keys_alt, perm_alt, cell, dist, pivots,
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
         out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched, clq0, clq1,
-        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info, lm_b16, xb_sortedB,
+        hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info, sball_b16,
+        sball_info, lm_b16, xb_sortedB,
         fin_x, fin_idx;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;

@@ -220,7 +220,7 @@ int rnng_ctx_trim(rnng_ctx* c)
                           &c->clq0, &c->clq1, &c->hi_id, &c->hi_val, &c->hi_flag, &c->sflag, &c->vflag,
                           &c->items, &c->items_tmp, &c->sched_tmp, &c->sym, &c->shift_buf, &c->ball_b16,
                           &c->ball_info, &c->sball_b16, &c->sball_info, &c->lm_b16, &c->xb_sortedB, &c->fin_x,
-                          &c->fin_idx};
+                          &c->fin_idx, &c->part_k, &c->part_v, &c->part_f};
         for (DevBuf* b : bufs) b->release();
         if (c->host_stage.ptr) cudaFreeHost(c->host_stage.ptr);
         c->host_stage.ptr = nullptr;

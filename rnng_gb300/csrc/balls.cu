@@ -43,9 +43,10 @@ __device__ __forceinline__ int tri_index(int i, int j, int m)
 }
 
 // One block per parent cell: pairwise distances of its children's landmarks into
-// shared memory (upper triangle; a warp per pair, lanes over dimensions), then one
-// warp walks the greedy chain.
-__global__ void __launch_bounds__(256) k_chain_leaves(const float* __restrict__ L, int d,
+// shared memory (upper triangle; from rows staged in shared memory, a thread per pair,
+// or for wide rows a warp per pair with lanes over dimensions), then one warp walks the
+// greedy chain.
+__global__ void __launch_bounds__(256) k_chain_leaves(const float* __restrict__ L, int d, bool staged,
                                                       const int32_t* __restrict__ m2,
                                                       const int32_t* __restrict__ m2_off, int32_t* __restrict__ rank)
 {
@@ -57,19 +58,50 @@ __global__ void __launch_bounds__(256) k_chain_leaves(const float* __restrict__ 
         if (threadIdx.x == 0) rank[base] = base;
         return;
     }
-    for (int p = warp; p < m * m; p += nw) {
-        const int i = p / m, j = p % m;
-        if (j <= i) continue;  // warp-uniform
-        const float* a = L + (int64_t)(base + i) * d;
-        const float* b = L + (int64_t)(base + j) * d;
-        float s = 0.f;
-        for (int k = lane; k < d; k += 32) {
-            const float t = a[k] - b[k];
-            s = fmaf(t, t, s);
+    if (staged) {
+        // the children's landmark rows in shared memory (rows d + 1 floats apart), then one
+        // thread per pair
+        float* R = Dm + kChainMax * (kChainMax - 1) / 2;
+        for (int e = threadIdx.x; e < m * d; e += blockDim.x) R[(e / d) * (d + 1) + e % d] = L[(int64_t)base * d + e];
+        __syncthreads();
+        for (int p = threadIdx.x; p < m * (m - 1) / 2; p += blockDim.x) {
+            // p -> (i, j), i < j, in the order of tri_index
+            int i = 0, rest = p;
+            while (rest >= m - 1 - i) {
+                rest -= m - 1 - i;
+                ++i;
+            }
+            const int j = i + 1 + rest;
+            const float* a = R + i * (d + 1);
+            const float* b = R + j * (d + 1);
+            float s0 = 0.f, s1 = 0.f;
+            int k = 0;
+            for (; k + 1 < d; k += 2) {
+                const float t0 = a[k] - b[k], t1 = a[k + 1] - b[k + 1];
+                s0 = fmaf(t0, t0, s0);
+                s1 = fmaf(t1, t1, s1);
+            }
+            if (k < d) {
+                const float t0 = a[k] - b[k];
+                s0 = fmaf(t0, t0, s0);
+            }
+            Dm[p] = s0 + s1;
         }
+    } else {
+        for (int p = warp; p < m * m; p += nw) {
+            const int i = p / m, j = p % m;
+            if (j <= i) continue;  // warp-uniform
+            const float* a = L + (int64_t)(base + i) * d;
+            const float* b = L + (int64_t)(base + j) * d;
+            float s = 0.f;
+            for (int k = lane; k < d; k += 32) {
+                const float t = a[k] - b[k];
+                s = fmaf(t, t, s);
+            }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) Dm[tri_index(i, j, m)] = s;
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) Dm[tri_index(i, j, m)] = s;
+        }
     }
     __syncthreads();
     if (warp != 0) return;
@@ -130,31 +162,39 @@ struct CoverState {
     float pick_v;
 };
 
-// distance of item r (row x, d floats) to row v, sequential fmaf over the dimensions
+// distance of item r (row x, d floats) to row v: fmaf over the dimensions in four interleaved
+// partial sums (any order is covered by the radii's widening)
 __device__ __forceinline__ float row_dist(const float* __restrict__ x, const float* __restrict__ v, int d)
 {
-    float s = 0.f;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = 0;
     if ((d & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(v)) & 15) == 0) {
         const float4* x4 = reinterpret_cast<const float4*>(x);
         const float4* v4 = reinterpret_cast<const float4*>(v);
-        for (int k = 0; k < (d >> 2); ++k) {
-            const float4 a = x4[k], b = v4[k];
-            float t = a.x - b.x;
-            s = fmaf(t, t, s);
-            t = a.y - b.y;
-            s = fmaf(t, t, s);
-            t = a.z - b.z;
-            s = fmaf(t, t, s);
-            t = a.w - b.w;
-            s = fmaf(t, t, s);
+        for (int q = 0; q < (d >> 2); ++q) {
+            const float4 a = x4[q], b = v4[q];
+            const float t0 = a.x - b.x, t1 = a.y - b.y, t2 = a.z - b.z, t3 = a.w - b.w;
+            s0 = fmaf(t0, t0, s0);
+            s1 = fmaf(t1, t1, s1);
+            s2 = fmaf(t2, t2, s2);
+            s3 = fmaf(t3, t3, s3);
         }
+        k = d;
     } else {
-        for (int k = 0; k < d; ++k) {
-            const float t = x[k] - v[k];
-            s = fmaf(t, t, s);
+#pragma unroll 4
+        for (; k + 3 < d; k += 4) {
+            const float t0 = x[k] - v[k], t1 = x[k + 1] - v[k + 1], t2 = x[k + 2] - v[k + 2], t3 = x[k + 3] - v[k + 3];
+            s0 = fmaf(t0, t0, s0);
+            s1 = fmaf(t1, t1, s1);
+            s2 = fmaf(t2, t2, s2);
+            s3 = fmaf(t3, t3, s3);
         }
     }
-    return sqrtf(s);
+    for (; k < d; ++k) {
+        const float t = x[k] - v[k];
+        s0 = fmaf(t, t, s0);
+    }
+    return sqrtf((s0 + s1) + (s2 + s3));
 }
 
 // block-wide (max value, index) with ties to the smaller index; result in st.pick / st.pick_v
@@ -191,9 +231,11 @@ __device__ __forceinline__ void cover_argmax(CoverState& st, float v, int i)
 
 // Up to K groups of the n items; centres into cen[K][d] (global, owned by the block),
 // radii into rad[K] (-1: no group).  `cbuf` is d floats of shared memory for the centroid.
+// With `sums` (K d floats of shared memory, or null) the group centroids take one pass over
+// the items instead of one per group.
 __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int ld, const float* __restrict__ irad,
-                             int n, int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ cen,
-                             float* __restrict__ rad)
+                             int n, int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ sums,
+                             float* __restrict__ cen, float* __restrict__ rad)
 {
     // item r is src[r ld .. r ld + d)
     const int t = threadIdx.x;
@@ -227,26 +269,37 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
         }
         if (ng + 1 < K) cover_argmax(st, mine ? dm : -1.f, t);
     }
-    if (mine) st.label[t] = lab;
+    if (mine) {
+        st.label[t] = lab;
+        atomicAdd(&st.count[lab], 1);
+    }
+    if (sums)
+        for (int e = t; e < ng * d; e += blockDim.x) sums[e] = 0.f;
     __syncthreads();
     // group centroids (thread k sums dimension k over the group's items), then radii
-    for (int g = 0; g < ng; ++g) {
-        for (int k = t; k < d; k += blockDim.x) {
-            float a = 0.f;
-            int c = 0;
-            for (int r = 0; r < n; ++r)
-                if (st.label[r] == g) {
-                    a += src[(int64_t)r * ld + k];
-                    ++c;
-                }
-            cen[(int64_t)g * d + k] = c ? a / (float)c : 0.f;
+    if (sums) {
+        for (int k = t; k < d; k += blockDim.x)
+            for (int r = 0; r < n; ++r) sums[st.label[r] * d + k] += src[(int64_t)r * ld + k];
+        __syncthreads();
+        for (int e = t; e < ng * d; e += blockDim.x) {
+            const int c = st.count[e / d];
+            cen[e] = c ? sums[e] / (float)c : 0.f;
+        }
+    } else {
+        for (int g = 0; g < ng; ++g) {
+            const int c = st.count[g];
+            for (int k = t; k < d; k += blockDim.x) {
+                float a = 0.f;
+                for (int r = 0; r < n; ++r)
+                    if (st.label[r] == g) a += src[(int64_t)r * ld + k];
+                cen[(int64_t)g * d + k] = c ? a / (float)c : 0.f;
+            }
         }
     }
     __syncthreads();
     if (mine) {
         const float rr = row_dist(xr, cen + (int64_t)lab * d, d) + ir;
         atomicMax(&st.rad_bits[lab], __float_as_uint(rr));
-        atomicAdd(&st.count[lab], 1);
     }
     __syncthreads();
     if (t < K) rad[t] = (t < ng && st.count[t] > 0) ? __uint_as_float(st.rad_bits[t]) * grow + 1e-30f : -1.f;
@@ -256,16 +309,17 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
 // One block per tile.  Output: centres [T][kTileBalls][d], radii [T][kTileBalls] (-1 =
 // unused).  With staged = true the tile's rows are first copied to shared memory (rows
 // d + 1 floats apart, so that the threads' row walks hit distinct banks), which every
-// pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), plus
-// kTile (d + 1) floats when staged.
+// pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), kTileBalls d
+// floats with use_sums (group sums), and kTile (d + 1) floats when staged.
 __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d,
-                                                              float grow, bool staged, float* __restrict__ cen,
-                                                              float* __restrict__ rad)
+                                                              float grow, bool staged, bool use_sums,
+                                                              float* __restrict__ cen, float* __restrict__ rad)
 {
     __shared__ CoverState st;
     extern __shared__ __align__(16) float dsm[];
     float* cbuf = dsm;
-    float* tile_rows = dsm + ((d + 3) & ~3);
+    float* sums = dsm + ((d + 3) & ~3);  // kTileBalls d floats when use_sums
+    float* tile_rows = sums + (use_sums ? kTileBalls * d : 0);
     const int64_t t = blockIdx.x;
     const int64_t r0 = t * kTile;
     const int nitems = (int)min((int64_t)kTile, n - r0);
@@ -291,15 +345,15 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
         src = tile_rows;
         ld = d + 1;
     }
-    cover_groups(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, cen + t * kTileBalls * d,
-                 rad + t * kTileBalls);
+    cover_groups(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, use_sums ? sums : nullptr,
+                 cen + t * kTileBalls * d, rad + t * kTileBalls);
 }
 
 // One block per super-tile: kSuperBalls balls over its tiles' valid balls (items with
-// their radii).  Dynamic shared memory: d floats.
+// their radii).  Dynamic shared memory: d floats, plus kSuperBalls d with use_sums.
 __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __restrict__ tcen,
                                                                const float* __restrict__ trad, int64_t T, int d,
-                                                               float grow, float* __restrict__ work,
+                                                               float grow, bool use_sums, float* __restrict__ work,
                                                                float* __restrict__ scen, float* __restrict__ srad)
 {
     __shared__ CoverState st;
@@ -327,7 +381,8 @@ __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __re
         for (int j = threadIdx.x; j < d; j += blockDim.x)
             items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
     __syncthreads();
-    cover_groups(st, items, d, irad, m, d, kSuperBalls, grow, dsm, scen + s * kSuperBalls * d, srad + s * kSuperBalls);
+    cover_groups(st, items, d, irad, m, d, kSuperBalls, grow, dsm, use_sums ? dsm + ((d + 3) & ~3) : nullptr,
+                 scen + s * kSuperBalls * d, srad + s * kSuperBalls);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -783,8 +838,9 @@ static int bits_for_tiles(int64_t T)
 void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchild, const int32_t* child_off,
                   int ncells, int32_t* rank)
 {
-    const size_t smem = sizeof(float) * kChainMax * (kChainMax - 1) / 2;
-    k_chain_leaves<<<ncells, 256, smem, c->stream>>>(lm_rows, d, nchild, child_off, rank); ++c->launches;
+    const bool staged = d <= 128;  // 64 rows of d + 1 floats next to the distances: at most 41 KB
+    const size_t smem = sizeof(float) * (kChainMax * (kChainMax - 1) / 2 + (staged ? kChainMax * (d + 1) : 0));
+    k_chain_leaves<<<ncells, 256, smem, c->stream>>>(lm_rows, d, staged, nchild, child_off, rank); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }
 
@@ -800,13 +856,19 @@ void build_covers(rnng_ctx* c, Layout& L)
     // tiles staged in shared memory up to 128 dimensions (64 KB; larger tiles read through L1)
     const bool staged = L.d <= 128;
     const size_t csm = sizeof(float) * (size_t)((L.d + 3) & ~3);
-    const size_t tsm = csm + (staged ? sizeof(float) * kTile * (size_t)(L.d + 1) : 0);
+    // group sums in shared memory up to 32 KB
+    const bool tsums = (size_t)kTileBalls * L.d * sizeof(float) <= 32768;
+    const bool ssums = (size_t)kSuperBalls * L.d * sizeof(float) <= 32768;
+    const size_t tsm = csm + (tsums ? sizeof(float) * kTileBalls * (size_t)L.d : 0) +
+                       (staged ? sizeof(float) * kTile * (size_t)(L.d + 1) : 0);
+    const size_t ssm = csm + (ssums ? sizeof(float) * kSuperBalls * (size_t)L.d : 0);
     RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-    RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
-    k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, c->tile_lo.as<float>(),
-                                                           c->tile_hi.as<float>()); ++c->launches;
-    k_super_balls<<<(unsigned)L.S, kCoverThreads, csm, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d,
-                                                            grow, c->pivots.as<float>(), c->super_lo.as<float>(),
+    RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, tsums,
+                                                           c->tile_lo.as<float>(), c->tile_hi.as<float>());
+    ++c->launches;
+    k_super_balls<<<(unsigned)L.S, kCoverThreads, ssm, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d,
+                                                            grow, ssums, c->pivots.as<float>(), c->super_lo.as<float>(),
                                                             c->super_hi.as<float>()); ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }

@@ -101,7 +101,7 @@ struct rnng_ctx {
         tile_lo, tile_hi, super_lo, super_hi, pair_list, super_list, counters, edges_u, edges_v, edges_w,
         out_u, out_v, out_w, cub_tmp, cand, aux0, aux1, aux2, aux3, aux4, aux5, aux6, aux7, sched, clq0, clq1,
         hi_id, hi_val, hi_flag, sflag, vflag, items, items_tmp, sched_tmp, sym, shift_buf, ball_b16, ball_info, sball_b16,
-        sball_info, lm_b16, xb_sortedB,
+        sball_info, lm_b16, xb_sortedB, part_k, part_v, part_f,
         fin_x, fin_idx;
     rnng::DevBuf host_stage;  // pinned host memory (cudaMallocHost), not device memory
     unsigned long long edge_cap_hint = 0, cand_cap_hint = 0;

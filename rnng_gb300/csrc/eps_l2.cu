@@ -235,6 +235,48 @@ __global__ void k_finalize_edges(const uint32_t* __restrict__ si, const uint32_t
     }
 }
 
+// Rows of the current order whose cell splits at this level (flag 1), and the others (0).
+__global__ void k_active_rows(const uint64_t* __restrict__ skeys, int64_t n, const int32_t* __restrict__ nchild,
+                              int32_t* __restrict__ flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = nchild[skeys[i] >> 32] > 1 ? 1 : 0;
+}
+
+// The active rows (those whose cell splits), in order: their positions, input rows and keys.
+__global__ void k_compact_active(const uint64_t* __restrict__ skeys, const int32_t* __restrict__ order, int64_t n,
+                                 const int32_t* __restrict__ flag, const int32_t* __restrict__ pos,
+                                 uint64_t* __restrict__ ckey, int32_t* __restrict__ crow, int32_t* __restrict__ cidx)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) {
+            const int32_t j = pos[i];
+            ckey[j] = skeys[i];
+            crow[j] = order[i];
+            cidx[j] = (int32_t)i;
+        }
+}
+
+// The level's new order: an inactive row keeps its place and its distance key under its
+// cell's single child (the cell does not move and keeps its order); the sorted active
+// rows fill the active places in order.
+__global__ void k_place_rows(int64_t n, const int32_t* __restrict__ flag, const int32_t* __restrict__ child_off,
+                             const int32_t* __restrict__ rank, const uint64_t* __restrict__ ck,
+                             const int32_t* __restrict__ cv, const int32_t* __restrict__ cidx, int64_t m,
+                             uint64_t* __restrict__ skeys, int32_t* __restrict__ order)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+        if (!flag[i]) {
+            const uint64_t k = skeys[i];
+            skeys[i] = ((uint64_t)(uint32_t)rank[child_off[k >> 32]] << 32) | (k & 0xffffffffull);
+        }
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += stride) {
+        skeys[cidx[j]] = ck[j];
+        order[cidx[j]] = cv[j];
+    }
+}
+
 __global__ void k_iota_keys(int32_t* __restrict__ order, uint64_t* __restrict__ keys, int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -432,8 +474,19 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         k_cell_bounds<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(skeys, n, cstart, cend); ++c->launches;
         k_split_plan<<<(unsigned)ceil_div(ncells, 256), 256, 0, s>>>(cstart, cend, ncells, nchild); ++c->launches;
         exclusive_scan_i32(c, nchild, child_off, ncells + 1);
-        int32_t total = 0;
+        int32_t total = 0, active = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, child_off + ncells, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        // rows whose cell splits: after the first levels a few cells, so only their rows are
+        // sorted (the others keep their places)
+        c->part_f.reserve(sizeof(int32_t) * 2 * (size_t)(n + 1));
+        int32_t* aflag = c->part_f.as<int32_t>();
+        int32_t* apos = aflag + n + 1;
+        if (levels >= 2) {
+            k_active_rows<<<grid_for(c, n, 256), 256, 0, s>>>(skeys, n, nchild, aflag); ++c->launches;
+            RNNG_CUDA(cudaMemsetAsync(aflag + n, 0, sizeof(int32_t), s));
+            exclusive_scan_i32(c, aflag, apos, n + 1);
+            RNNG_CUDA(cudaMemcpyAsync(&active, apos + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        }
         unsigned long long hs[2] = {0ull, 0ull};
         if (levels == 0)
             RNNG_CUDA(cudaMemcpyAsync(hs, scr, (b16 ? 2 : 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
@@ -456,11 +509,33 @@ Layout build_layout(rnng_ctx* c, const float* dX, int64_t n, int d, float radius
         k_gather_rows<<<grid_for(c, (int64_t)total * d, 256), 256, 0, s>>>(dX, d, lm_idx, total, lm_rows); ++c->launches;
         // children ordered along a greedy nearest-neighbour chain of their landmarks
         chain_leaves(c, lm_rows, d, nchild, child_off, (int)ncells, c->aux5.as<int32_t>());
-        launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, c->aux5.as<int32_t>(), shift, nkeys,
-                      nvals);
-        // by child, then by distance (the order inside a cell shapes its tiles: a coarser
-        // distance key left 4.6 % more tile pairs at K2)
-        sort_pairs_u64(c, nkeys, skeys, nvals, order, n, 32 + bits_for(total));
+        int32_t* rank = c->aux5.as<int32_t>();
+        if (levels < 2 || 4 * (int64_t)active > n) {
+            launch_assign(c, dX, order, n, d, lm_rows, total, skeys, child_off, rank, shift, nkeys, nvals);
+            // by child, then by distance (the order inside a cell shapes its tiles: a coarser
+            // distance key left 4.6 % more tile pairs at K2)
+            sort_pairs_u64(c, nkeys, skeys, nvals, order, n, 32 + bits_for(total));
+        } else {
+            // few rows in splitting cells: assign and sort only those, in place of their cells
+            const int64_t m = active, mm = std::max<int64_t>(m, 1);
+            c->part_k.reserve(sizeof(uint64_t) * 3 * (size_t)mm);
+            c->part_v.reserve(sizeof(int32_t) * 4 * (size_t)mm);
+            uint64_t* ckey = c->part_k.as<uint64_t>();
+            uint64_t* ck = ckey + mm;
+            uint64_t* ck2 = ck + mm;
+            int32_t* crow = c->part_v.as<int32_t>();
+            int32_t* cv = crow + mm;
+            int32_t* cv2 = cv + mm;
+            int32_t* cidx = cv2 + mm;
+            if (m > 0) {
+                k_compact_active<<<grid_for(c, n, 256), 256, 0, s>>>(skeys, order, n, aflag, apos, ckey, crow, cidx);
+                ++c->launches;
+                launch_assign(c, dX, crow, m, d, lm_rows, total, ckey, child_off, rank, shift, ck, cv);
+                sort_pairs_u64(c, ck, ck2, cv, cv2, m, 32 + bits_for(total));
+            }
+            k_place_rows<<<grid_for(c, n, 256), 256, 0, s>>>(n, aflag, child_off, rank, ck2, cv2, cidx, m, skeys, order);
+            ++c->launches;
+        }
         ncells = total;
     }
     L.num_cells = ncells;

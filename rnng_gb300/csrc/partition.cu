@@ -57,6 +57,12 @@ __global__ void __launch_bounds__(256) k_assign(const float* __restrict__ X, con
     for (int r = 0; r < 4; ++r) need |= (rhi[r] - rlo[r] > 1) ? 1 : 0;
     if (!__syncthreads_or(need)) hi = lo;
     for (int64_t c0 = lo; c0 < hi; c0 += kDCols) {
+        // rows of a compacted list can come from far-apart cells: skip chunks no row may use
+        int use = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            use |= ((!row_key || rhi[r] - rlo[r] > 1) && rlo[r] < c0 + kDCols && rhi[r] > c0) ? 1 : 0;
+        if (!__syncthreads_or(use)) continue;
         float acc[4][4];
         dist_block(sm, X, rowmap, r0, nrows, d, C, c0, hi, acc);
 #pragma unroll
@@ -181,9 +187,20 @@ __global__ void __launch_bounds__(256) k_assign_mma(const float* __restrict__ X,
         rlo[h] = cell_off[cell];
         rhi[h] = cell_off[cell + 1];
     }
-    // blocks whose rows all sit in cells that do not split keep their keys: no distances
+    // blocks whose rows all sit in cells that do not split keep their keys: no rows read,
+    // no distances (most blocks at the deeper levels)
     const int need = (rv[0] && rhi[0] - rlo[0] > 1) || (rv[1] && rhi[1] - rlo[1] > 1);
-    if (!__syncthreads_or(need)) hi = lo;
+    if (!__syncthreads_or(need)) {
+        if (t == 0)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                if (rv[h]) {
+                    const int col = col_rank ? col_rank[rlo[h]] : rlo[h];
+                    keys_out[row[h]] = ((uint64_t)(uint32_t)col << 32) | (row_key[row[h]] & 0xffffffffull);
+                    vals_out[row[h]] = rowmap ? rowmap[row[h]] : (int32_t)row[h];
+                }
+        return;
+    }
     uint32_t af[KP][2][4];
     float xn[2] = {0.f, 0.f};
 #pragma unroll
@@ -196,7 +213,25 @@ __global__ void __launch_bounds__(256) k_assign_mma(const float* __restrict__ X,
     }
     float best[2] = {INFINITY, INFINITY};
     int bidx[2] = {0, 0};
-    for (int c0 = lo; c0 < hi; c0 += 32) {
+    // this warp's column range: the union of its rows' ranges (rows of a compacted list can
+    // come from far-apart cells; chunks that none of the warp's rows may use are skipped)
+    int wlo = hi, whi = lo;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (rv[h] && rhi[h] - rlo[h] > 1) {
+            wlo = min(wlo, rlo[h]);
+            whi = max(whi, rhi[h]);
+        }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        wlo = min(wlo, __shfl_xor_sync(0xffffffffu, wlo, o));
+        whi = max(whi, __shfl_xor_sync(0xffffffffu, whi, o));
+    }
+    for (int c0 = wlo; c0 < whi; c0 += 32) {
+        bool use = false;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) use |= rv[h] && rhi[h] - rlo[h] > 1 && rlo[h] < c0 + 32 && rhi[h] > c0;
+        if (!__any_sync(0xffffffffu, use)) continue;
         float acc[4][4];
 #pragma unroll
         for (int nt = 0; nt < 4; ++nt)
@@ -208,7 +243,7 @@ __global__ void __launch_bounds__(256) k_assign_mma(const float* __restrict__ X,
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
                 const int col = c0 + 8 * nt + g;
-                bf[nt] = col < hi ? Cb[(int64_t)col * (4 * KP) + 4 * kp + t] : make_uint4(0u, 0u, 0u, 0u);
+                bf[nt] = col < whi ? Cb[(int64_t)col * (4 * KP) + 4 * kp + t] : make_uint4(0u, 0u, 0u, 0u);
             }
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
@@ -222,7 +257,7 @@ __global__ void __launch_bounds__(256) k_assign_mma(const float* __restrict__ X,
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int col = c0 + 8 * nt + 2 * t + e;
-                const float cn = col < hi ? cnorm[col] : 0.f;
+                const float cn = col < whi ? cnorm[col] : 0.f;
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float dist = fmaf(-2.f, acc[nt][2 * h + e], xn[h] + cn);

@@ -118,6 +118,11 @@ int rnng_ctx_trim(rnng_ctx* ctx);
  * (rnng_gb300/gram_tuning.json, read when the context is created; $RNNG_GRAM_TUNING
  * names another file) or the default; all three 0 restores the table. */
 int rnng_ctx_set_gram_tuning(rnng_ctx* ctx, int nt, int chunk, int slots);
+/* No counterpart in RNNG: a drill of the failure handling.  While on, the tensor-core Gram
+ * kernel's epilogue waits on a barrier that nothing arrives on; its bounded wait (about
+ * one second) runs out, the kernel winds down (copies and MMAs in flight drained, tensor
+ * memory freed), and the call returns RNNG_ERR_DEVICE.  The context stays usable. */
+int rnng_ctx_fault_drill(rnng_ctx* ctx, int on);
 
 /* Epsilon graph, L2 ------------------------------------------------------------------------
  * Replaces the neighbour search of the drivers: CoverTree::build + radius_query per point
@@ -193,6 +198,16 @@ int rnng_rips_edges(rnng_ctx* ctx, int64_t n, const int64_t* ids, const uint8_t*
  * coordinate has none there; drop such rows' (i, i, 0) entries to match.) */
 int rnng_graph_finalize(rnng_ctx* ctx, const rnng_edges* edges, int64_t num_vertices, unsigned flags,
                         rnng_edges* out);
+
+/* Diagnostic, no counterpart in RNNG: one tile pair through the tensor-core Gram kernel of
+ * rnng_eps_graph_l2's BF16 mode, to measure the tensor cores' FP32 accumulation against the
+ * error bound the candidate test assumes.  X: 256 x d host floats (d = 64, 128, 192 or
+ * 256), rows 0..127 the row tile, rows 128..255 the column tile.  Outputs (host):
+ * G[i * 128 + j] = the raw accumulator of row i against row 128 + j; Xb (256 x d) = the
+ * BF16 operand rows as the kernel used them (shifted by the rounded column means, as
+ * floats); rowinfo (256 x 4 floats) = per row {BF16 norm, error radius a, accumulation
+ * bound q, column term}.  The candidate test is sound when |2 (G - Xb_i . Xb_j)| <= q_i + q_j. */
+int rnng_gram_probe_bf16(rnng_ctx* ctx, const float* X, int64_t d, float* G, float* Xb, float* rowinfo);
 
 int rnng_edges_free(rnng_edges* e);
 int rnng_simplices_free(rnng_simplices* s);

@@ -35,7 +35,7 @@ MODES = {"fp32": 0, "bf16": 1}
 # every entry point include/rnng_gpu.h declares
 EXPORTS = [
     "rnng_ctx_create", "rnng_ctx_destroy", "rnng_last_error", "rnng_get_stats", "rnng_ctx_stream", "rnng_ctx_trim",
-    "rnng_ctx_set_gram_tuning",
+    "rnng_ctx_set_gram_tuning", "rnng_gram_probe_bf16", "rnng_ctx_fault_drill",
     "rnng_eps_graph_l2", "rnng_radius_query_l2", "rnng_voronoi_l2", "rnng_eps_graph_edit", "rnng_rips_l2",
     "rnng_graph_finalize", "rnng_edges_free", "rnng_simplices_free", "rnng_eps_graph_l2_static",
     "rnng_voronoi_edit", "rnng_rips_edges",
@@ -92,6 +92,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.rnng_ctx_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.rnng_ctx_trim.argtypes = [vp]
     L.rnng_ctx_set_gram_tuning.argtypes = [vp, ip, ip, ip]
+    L.rnng_gram_probe_bf16.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.rnng_ctx_fault_drill.argtypes = [vp, ip]
     L.rnng_eps_graph_l2.argtypes = [vp, vp, vp, i64, i64, f32, ip, u32, ctypes.POINTER(Edges)]
     L.rnng_radius_query_l2.argtypes = [vp, vp, vp, i64, vp, vp, i64, i64, f32, u32, ctypes.POINTER(Edges)]
     L.rnng_voronoi_l2.argtypes = [vp, vp, i64, vp, i64, i64, u32, vp, vp]
@@ -178,6 +180,21 @@ class Context:
         """Forces the Gram kernel's column tiles per item, queue chunk and B slots (0: the
         tuning table's value or the default)."""
         self._check(self.lib.rnng_ctx_set_gram_tuning(self.h, nt, chunk, slots), self.h)
+
+    def fault_drill(self, on: bool) -> None:
+        """rnng_ctx_fault_drill: the Gram kernel's bounded wait runs out on purpose."""
+        self._check(self.lib.rnng_ctx_fault_drill(self.h, 1 if on else 0), self.h)
+
+    def gram_probe_bf16(self, X):
+        """One tile pair through the Gram kernel (rnng_gram_probe_bf16): X is 256 x d; returns
+        (G 128 x 128 raw accumulators, Xb 256 x d BF16 operand rows, rowinfo 256 x 4)."""
+        X = np.ascontiguousarray(X, np.float32)
+        n, d = X.shape
+        G = np.zeros((128, 128), np.float32)
+        Xb = np.zeros((n, d), np.float32)
+        info = np.zeros((n, 4), np.float32)
+        self._check(self.lib.rnng_gram_probe_bf16(self.h, _ptr(X), d, _ptr(G), _ptr(Xb), _ptr(info)), self.h)
+        return G, Xb, info
 
     def stream(self) -> int:
         p = ctypes.c_void_p()

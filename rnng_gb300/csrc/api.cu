@@ -207,6 +207,13 @@ int rnng_ctx_set_gram_tuning(rnng_ctx* c, int nt, int chunk, int slots)
     return RNNG_OK;
 }
 
+int rnng_ctx_fault_drill(rnng_ctx* c, int on)
+{
+    if (!c) return RNNG_ERR_INVALID;
+    c->fault_drill = on != 0;
+    return RNNG_OK;
+}
+
 int rnng_ctx_trim(rnng_ctx* c)
 {
     if (!c) return RNNG_ERR_INVALID;

@@ -123,6 +123,7 @@ struct rnng_ctx {
     bool have_events = false;
     std::vector<rnng::GramTune> gram_table;  // loaded at creation
     rnng::GramTune gram_force;                // rnng_ctx_set_gram_tuning (0 fields: not forced)
+    bool fault_drill = false;                 // rnng_ctx_fault_drill
 };
 
 namespace rnng {

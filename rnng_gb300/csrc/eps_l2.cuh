@@ -37,6 +37,7 @@ struct Layout {
     int item_tiles = 1;
     int gram_chunk = 64;
     int gram_slots = 0;
+    float* gram_raw = nullptr;  // diagnostic: the Gram kernel writes its raw accumulators here (n_pad x n_pad)
     // build_layout stopped before the partition: the screen found a non-finite input value
     bool nonfinite = false;
     float maxabs = 0.f;  // largest |coordinate| (d <= 256 only)

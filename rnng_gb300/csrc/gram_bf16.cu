@@ -45,6 +45,7 @@
 
 #include "common.cuh"
 #include "eps_l2.cuh"
+#include "kernels_misc.cuh"
 
 namespace rnng {
 
@@ -75,8 +76,8 @@ constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared mem
 struct GramSmem {
     uint32_t colinfo, bars, misc, cq, a_tile, b_ring, slot_bytes, total;
     int nslots;
-    // a_full/empty, b_full/empty, tfull/tempty, drain, chunk ring full/empty
-    static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1 + 2 * kChunkRing;
+    // a_full/empty, b_full/empty, tfull/tempty, drain, chunk ring full/empty, drill
+    static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1 + 2 * kChunkRing + 1;
     // max_slots > 0 caps the B ring (a tuning knob); the ring always holds at least 2 slots
     __host__ __device__ static GramSmem make(int kch, int nt, int max_slots = 0)
     {
@@ -353,14 +354,16 @@ __device__ __forceinline__ bool take_chunk(uint64_t* cq_full, uint64_t* cq_empty
 // tiles come from tmapB with the column terms folded into their padding (k_to_bf16), so
 // the accumulator already holds g - u_j / 2 and the test needs no u_j
 // F8: 8-bit operands (E4M3; 128 per 128-byte chunk row, K = 32 per MMA), same byte layout.
-template <int KCH, int NT, bool FOLD, bool F8>
+// RAW: the diagnostic form of rnng_gram_probe_bf16, which also writes the raw accumulators.
+template <int KCH, int NT, bool FOLD, bool F8, bool RAW = false>
 __global__ void __maxnreg__(kGramMaxRegs)
     k_gram_bf16(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap tmapB,
                 const int4* __restrict__ items, unsigned long long nitems,
                 const float4* __restrict__ rowinfo, const float* __restrict__ ucol,
                 const float2* __restrict__ tileinfo, int64_t n, float eps_p, float kappa, uint2* __restrict__ cand,
                 unsigned long long* __restrict__ cand_count, unsigned long long cand_cap,
-                unsigned long long* __restrict__ qhead, int chunk, int max_slots, int* __restrict__ fault)
+                unsigned long long* __restrict__ qhead, int chunk, int max_slots, int* __restrict__ fault,
+                float* __restrict__ raw, int64_t raw_ld, int drill)
 {
     constexpr int kAcc = kTmemCols / (kAccCols * NT);  // accumulators in flight
     constexpr uint32_t kIdesc = F8 ? gram_idesc_f8(NT) : gram_idesc(NT);
@@ -379,6 +382,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
     uint64_t* cq_full = drain + 1;             // chunk ring: posted by the producer
     uint64_t* cq_empty = cq_full + kChunkRing; // read by the MMA thread and every epilogue warp
     volatile long long* cqv = (volatile long long*)(sm + SL.cq);  // chunk's first item, -1: queue empty
+    uint64_t* drill_bar = cq_empty + kChunkRing;  // nothing ever arrives on it (rnng_ctx_fault_drill)
     // ring slots: one item (all K-chunks of its NT B tiles) per slot
     const int nslots = SL.nslots;
     const uint32_t slot_bytes = SL.slot_bytes;
@@ -407,6 +411,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
             mbar_init(&cq_full[k], 1);
             mbar_init(&cq_empty[k], 1 + kEpiWarps);
         }
+        mbar_init(drill_bar, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -656,7 +661,13 @@ __global__ void __maxnreg__(kGramMaxRegs)
         uint32_t w = 0;
         uint32_t local = 0;  // item index in the CTA's sequence
         ItemPrefetch pf;
-        bool have = take_next();
+        if (drill) {
+            // failure drill: wait on a barrier that nothing arrives on; the bounded wait runs
+            // out, records the fault and raises the abort flag, and the whole CTA winds down
+            const bool ok_ = lane == 0 ? mbar_wait(drill_bar, 0, abort_flag, fault, 11) : false;
+            alive = __shfl_sync(0xffffffffu, ok_ ? 1 : 0, 0) != 0;
+        }
+        bool have = alive && take_next();
         if (have) {
             w = c0 + goff;
             local = base + (uint32_t)goff;
@@ -750,6 +761,12 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 float g[32];
                 tmem_ld16x256b_x8(taddr + ((uint32_t)(16 * hh) << 16), g);
                 tmem_ld_wait();
+                if constexpr (RAW) {
+                    // diagnostic output (rnng_gram_probe_bf16): the accumulator as the tensor cores left it
+#pragma unroll
+                    for (int x = 0; x < 32; ++x)
+                        raw[(int64_t)(rb + 16 * hh + 8 * ((x >> 1) & 1)) * raw_ld + cb + 8 * (x >> 2) + (x & 1)] = g[x];
+                }
                 if (hh == 1) {
                     // accumulator slice read: hand it back to the MMA warp
                     tc_fence_before();
@@ -1309,21 +1326,22 @@ void prepare_bf16(rnng_ctx* c, Layout& L)
     RNNG_REQUIRE(r == CUDA_SUCCESS, RNNG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
 }
 
-template <int KCH, int NT, bool FOLD, bool F8>
+template <int KCH, int NT, bool FOLD, bool F8, bool RAW = false>
 static void gram_instance(bool launch, int grid, size_t smem, cudaStream_t s, const CUtensorMap& tm,
                           const CUtensorMap& tmb, const int4* items,
                           unsigned long long nitems, const float4* rowinfo, const float* ucol, const float2* tileinfo,
                           int64_t n, float eps_p, float kappa, uint2* cand, unsigned long long* cnt,
-                          unsigned long long ccap, unsigned long long* qhead, int chunk, int max_slots, int* fault)
+                          unsigned long long ccap, unsigned long long* qhead, int chunk, int max_slots, int* fault,
+                          float* raw, int64_t raw_ld, int drill)
 {
     if (!launch) {
-        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD, F8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+        RNNG_CUDA(cudaFuncSetAttribute(k_gram_bf16<KCH, NT, FOLD, F8, RAW>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return;
     }
-    k_gram_bf16<KCH, NT, FOLD, F8><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
+    k_gram_bf16<KCH, NT, FOLD, F8, RAW><<<grid, kGramThreads, smem, s>>>(tm, tmb, items, nitems, rowinfo, ucol, tileinfo, n,
                                                                 eps_p, kappa, cand, cnt, ccap, qhead, chunk,
-                                                                max_slots, fault);
+                                                                max_slots, fault, raw, raw_ld, drill);
 }
 
 // Sets the shared-memory size (launch = false) or launches the instance for (kch, nt, fold).
@@ -1339,6 +1357,23 @@ static void gram_dispatch_fold(int kch, int nt, Args... args)
             case 2: gram_instance<2, 1, FOLD, false>(args...); break;
             case 3: gram_instance<3, 1, FOLD, false>(args...); break;
             default: gram_instance<4, 1, FOLD, false>(args...); break;
+        }
+    }
+}
+
+// The diagnostic instances (raw accumulators out; no folded column terms, BF16 operands).
+template <class... Args>
+static void gram_dispatch_raw(int kch, int nt, Args... args)
+{
+    if (nt == 2) {
+        if (kch == 1) gram_instance<1, 2, false, false, true>(args...);
+        else gram_instance<2, 2, false, false, true>(args...);
+    } else {
+        switch (kch) {
+            case 1: gram_instance<1, 1, false, false, true>(args...); break;
+            case 2: gram_instance<2, 1, false, false, true>(args...); break;
+            case 3: gram_instance<3, 1, false, false, true>(args...); break;
+            default: gram_instance<4, 1, false, false, true>(args...); break;
         }
     }
 }
@@ -1461,8 +1496,14 @@ static unsigned long long gram_candidates(rnng_ctx* c, const Layout& L, const CU
     const size_t smem = layout.total + 1024;
     const int chunk = std::max(1, L.gram_chunk);
     unsigned long long* qhead = c->counters.as<unsigned long long>() + kSlotQueue;
-    gram_dispatch(fold, f8, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
-                  L.n, eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, qhead, chunk, L.gram_slots, c->fault_word);
+    if (L.gram_raw)
+        gram_dispatch_raw(kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo, L.n,
+                          eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, qhead, chunk, L.gram_slots, c->fault_word,
+                          (float*)nullptr, (int64_t)0, 0);
+    else
+        gram_dispatch(fold, f8, kchunks, nt, false, 0, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
+                      L.n, eps_p, 0.f, (uint2*)nullptr, cnt, 0ull, qhead, chunk, L.gram_slots, c->fault_word,
+                      (float*)nullptr, (int64_t)0, 0);
     // one CTA per SM, fewer when there are fewer chunks
     const int grid = (int)std::max<unsigned long long>(
         1, std::min<unsigned long long>((L.num_items + chunk - 1) / chunk, (unsigned long long)c->num_sms));
@@ -1476,9 +1517,14 @@ static unsigned long long gram_candidates(rnng_ctx* c, const Layout& L, const CU
         RNNG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaMemsetAsync(qhead, 0, sizeof(unsigned long long), s));
         RNNG_CUDA(cudaEventRecord(c->ev[9], s));
-        gram_dispatch(fold, f8, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol,
-                      tileinfo, L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, qhead, chunk, L.gram_slots,
-                      c->fault_word);
+        if (L.gram_raw)
+            gram_dispatch_raw(kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol, tileinfo,
+                              L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, qhead, chunk, L.gram_slots,
+                              c->fault_word, L.gram_raw, L.n_pad, 0);
+        else
+            gram_dispatch(fold, f8, kchunks, nt, true, grid, smem, s, tm, tmb, L.items, L.num_items, rowinfo, ucol,
+                          tileinfo, L.n, eps_p, kappa, c->cand.as<uint2>(), cnt, ccap, qhead, chunk, L.gram_slots,
+                          c->fault_word, (float*)nullptr, (int64_t)0, c->fault_drill ? 1 : 0);
         ++c->launches;
         RNNG_CUDA(cudaGetLastError());
         RNNG_CUDA(cudaEventRecord(c->ev[10], s));
@@ -1488,9 +1534,7 @@ static unsigned long long gram_candidates(rnng_ctx* c, const Layout& L, const CU
             float gms = 0.f;
             if (cudaEventElapsedTime(&gms, c->ev[9], c->ev[10]) == cudaSuccess) c->gram_ms += gms;
         }
-        int fw = 0;
-        RNNG_CUDA(cudaMemcpy(&fw, c->fault_word, sizeof(int), cudaMemcpyDeviceToHost));
-        RNNG_REQUIRE(fw == FAULT_NONE, RNNG_ERR_DEVICE, "Gram kernel: bounded wait ran out (fault word set)");
+        check_device_fault(c);  // a bounded wait that ran out: RNNG_ERR_DEVICE, the word cleared for the next call
         if (got <= ccap) {
             c->cand_cap_hint = std::max<unsigned long long>(c->cand_cap_hint, got + got / 8);
             break;
@@ -1547,3 +1591,56 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
 }
 
 }  // namespace rnng
+
+// Diagnostic entry point (include/rnng_gpu.h): one tile pair through the Gram kernel with
+// its raw accumulator written out.
+extern "C" int rnng_gram_probe_bf16(rnng_ctx* c, const float* X, int64_t d, float* G, float* Xb, float* rowinfo)
+{
+    using namespace rnng;
+    return guarded(c, [&] {
+        RNNG_REQUIRE(X && G && Xb && rowinfo, RNNG_ERR_INVALID, "null pointer");
+        RNNG_REQUIRE(d >= 64 && d <= kMaxDp && d % kChunkK == 0, RNNG_ERR_INVALID,
+                     "the probe takes d = 64, 128, 192 or 256");
+        cudaStream_t s = c->stream;
+        const int64_t n = 2 * kTile;
+        c->x_in.reserve(sizeof(float) * (size_t)n * d);
+        RNNG_CUDA(cudaMemcpyAsync(c->x_in.ptr, X, sizeof(float) * (size_t)n * d, cudaMemcpyHostToDevice, s));
+        Layout L;
+        L.n = n;
+        L.n_pad = n;
+        L.T = 2;
+        L.S = 1;
+        L.d = (int)d;
+        L.radius = 1.f;
+        L.Xs = c->x_in.as<float>();
+        prepare_bf16(c, L);  // the operands exactly as the epsilon graph builds them (shift, rounding, row terms)
+        const int4 item = make_int4(0, 1, -1, 0);
+        c->items.reserve(sizeof(int4));
+        RNNG_CUDA(cudaMemcpyAsync(c->items.ptr, &item, sizeof(int4), cudaMemcpyHostToDevice, s));
+        L.items = c->items.as<int4>();
+        L.num_items = 1;
+        L.item_tiles = gram_tune(c, 0, (int)d, 1).nt;
+        L.gram_chunk = 2;
+        c->aux7.reserve(sizeof(float) * (size_t)n * n);
+        L.gram_raw = c->aux7.as<float>();
+        RNNG_CUDA(cudaMemsetAsync(L.gram_raw, 0, sizeof(float) * (size_t)n * n, s));
+        c->counters.reserve(sizeof(unsigned long long) * kCounterSlots);
+        unsigned long long* cnt = c->counters.as<unsigned long long>() + 5;
+        const CUtensorMap& tm = *reinterpret_cast<const CUtensorMap*>(c->tmap);
+        const CUtensorMap& tmb = *reinterpret_cast<const CUtensorMap*>(c->tmapB);
+        gram_candidates(c, L, tm, tmb, (int)d / kChunkK, L.item_tiles, c->bf16_fold, false,
+                        (const float4*)c->bf16_rowinfo, (const float*)c->bf16_ucol, (const float2*)c->bf16_tileinfo,
+                        c->bf16_eps_p, cnt);
+        // G[i][j] = accumulator of A row i (input row i) and B row j (input row 128 + j)
+        for (int i = 0; i < kTile; ++i)
+            RNNG_CUDA(cudaMemcpyAsync(G + (int64_t)i * kTile, L.gram_raw + (int64_t)i * n + kTile, sizeof(float) * kTile,
+                                      cudaMemcpyDeviceToHost, s));
+        std::vector<__nv_bfloat16> xb((size_t)n * d);
+        RNNG_CUDA(cudaMemcpyAsync(xb.data(), c->xb_sorted.ptr, sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyDeviceToHost,
+                                  s));
+        RNNG_CUDA(cudaMemcpyAsync(rowinfo, c->bf16_rowinfo, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        RNNG_CUDA(cudaStreamSynchronize(s));
+        for (size_t k = 0; k < xb.size(); ++k) Xb[k] = __bfloat162float(xb[k]);
+        c->aux7.release();
+    });
+}

@@ -233,7 +233,7 @@ def main():
                     help="points of the descriptor workload (smaller sizes are for ncu captures only)")
     ap.add_argument("--k5-points", type=int, default=5_000_000,
                     help="points of the K5 workload (smaller sizes are for ncu captures only)")
-    ap.add_argument("--workload", default="k2", choices=["k1", "k2", "k3", "k4", "k5"],
+    ap.add_argument("--workload", default="k2", choices=["k1", "k2", "k3", "k4", "k5", "k2-dropin"],
                     help="k2 (default) is the headline; k1, k3, k4, k5 print the same line for the other "
                          "configurations (see SECONDARY)")
     args = ap.parse_args()
@@ -245,6 +245,10 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "k2-dropin":
+        if rank == 0:
+            run_dropin(args)
         return
     if args.workload != "k2":
         run_secondary(args, world, rank, local)
@@ -547,6 +551,48 @@ def run_secondary(args, world, rank, local):
     if dist:
         dist.destroy_process_group()
     ctx.close()
+
+
+def run_dropin(args):
+    """The headline workload through RNNG's own API: the landmark driver's calls (read_fvecs,
+    selection_sample, VoronoiDiagram, coalesce_cells, add_ghost_points_systolic, per-cell
+    CoverTree queries, Graph + redistribute_edges, write_file) compiled against the drop-in
+    headers (oracle/ref_harness.cpp, graph mode; 1,000 landmarks as RNNG's run of this
+    workload uses).  One run after a warm-up run; phase times from the harness."""
+    import re
+    import tempfile
+    import rnng_gb300
+    from rnng_gb300 import synth
+    rnng_gb300.build.build()
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin"], check=True)
+    harness = os.path.join(ROOT, "oracle", "_build", "dropin_harness")
+    x, radius = workload(args.points)
+    n = x.shape[0]
+    with tempfile.TemporaryDirectory() as tmp:
+        inp, out = os.path.join(tmp, "k2.fvecs"), os.path.join(tmp, "k2.mtx")
+        synth.write_fvecs(inp, x)
+        cmd = [harness, "graph", "l2", inp, repr(float(radius)), str(max(1, n // 1000)), "7", out]
+        runs = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            r = subprocess.run(cmd, capture_output=True, text=True, check=True)
+            runs.append((time.perf_counter() - t0, r.stderr))
+        wall, err = runs[-1]
+        phases = {m.group(2): float(m.group(1)) for m in re.finditer(r"\[phase ([\d.]+)\] (.+)", err)}
+        reported = int(re.search(r"edges=(\d+)", err).group(1))
+    edges = (reported - n) // 2
+    pipeline = sum(v for k, v in phases.items() if k not in ("read input", "wrote edges"))
+    line = {"metric": "eps-graph edges/s through RNNG's API (landmark driver calls, drop-in headers), 1M x 128",
+            "value": edges / pipeline, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": pipeline * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16", "data": "synthetic (seeded numpy, see rnng_gb300/synth.py)",
+            "config": config({"path": "drop-in headers, oracle/ref_harness.cpp graph mode", "landmarks": n // 1000,
+                              "edges": edges, "reported_edges": reported,
+                              "phases_s": {k: round(v, 4) for k, v in phases.items()}}, n),
+            "e2e": {"value": edges / wall, "unit": UNIT, "h2d_bytes_per_step": int(n * DIM * 4),
+                    "d2h_bytes_per_step": int(reported * 20), "seconds": wall,
+                    "note": "whole process: reads the .fvecs file, writes the text graph"}}
+    print(json.dumps(line), flush=True)
 
 
 def read_profile_traffic():

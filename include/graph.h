@@ -1,6 +1,7 @@
-// Drop-in edge list with the interface of RNNG's include/graph.h: construction sorts the
-// edges, redistribute_edges gives every rank both orientations of its vertices' edges
-// (sorted, duplicates removed), write_file prints a MatrixMarket-like text file.
+// Drop-in edge list with the interface of RNNG's include/graph.h: the edges are sorted
+// (RNNG sorts at construction; here before the first write), redistribute_edges gives
+// every rank both orientations of its vertices' edges (sorted, duplicates removed; on the
+// GPU at one rank), write_file prints a MatrixMarket-like text file.
 #ifndef RNNG_DROPIN_GRAPH_H_
 #define RNNG_DROPIN_GRAPH_H_
 
@@ -12,14 +13,14 @@ class Graph
     using Edge = std::tuple<Index, Index, Real>;
     using EdgeVector = std::vector<Edge>;
 
-    Graph(const EdgeVector& edges, Index num_vertices) : edges(edges), num_vertices(num_vertices)
-    {
-        std::sort(this->edges.begin(), this->edges.end());
-    }
+    // RNNG sorts here; the sort is deferred to the first use that can see the order
+    // (write_file), since redistribute_edges sorts again on the GPU anyway.
+    Graph(const EdgeVector& edges, Index num_vertices) : edges(edges), num_vertices(num_vertices) {}
 
     // "% n n m" then "u v w" with w printed "%.6f" (RNNG include/graph.hpp:1-17).
     void write_file(const char* fname) const
     {
+        ensure_sorted();
         FILE* f = std::fopen(fname, "w");
         assert((f != nullptr));
         std::fprintf(f, "%% %lld %lld %lld\n", (long long)num_vertices, (long long)num_vertices,
@@ -32,6 +33,7 @@ class Graph
     // rank 0, weights with six significant digits (RNNG include/graph.hpp:20-56).
     void write_file(const char* fname, MPI_Comm comm) const
     {
+        ensure_sorted();
         int rank = 0;
         MPI_Comm_rank(comm, &rank);
         Index total = (Index)edges.size();
@@ -56,14 +58,19 @@ class Graph
     }
 
     // Both orientations of every edge go to the owners of their first vertex (blocks of
-    // num_vertices / ranks), then sort and unique (RNNG include/graph.hpp:59-116).  The
-    // edges recorded by the drop-in queries already hold every self-loop; a whole-graph
-    // caller can get this list directly on the GPU with rnng_graph_finalize.
+    // num_vertices / ranks), then sort and unique (RNNG include/graph.hpp:59-116).  At one
+    // rank all of it runs on the GPU (rnng_graph_finalize with RNNG_FINALIZE_AS_GIVEN: the
+    // same tuples in the same order).  The edges recorded by the drop-in queries already
+    // hold every self-loop.
     void redistribute_edges(MPI_Comm comm)
     {
         int rank = 0, nranks = 1;
         MPI_Comm_rank(comm, &rank);
         MPI_Comm_size(comm, &nranks);
+        if (nranks == 1) {
+            finalize_on_gpu();
+            return;
+        }
         const Index chunk = std::max<Index>(1, num_vertices / nranks);
         auto owner = [&](Index x) { return (int)std::min<Index>(x / chunk, nranks - 1); };
         MPI_Datatype edge_t;
@@ -90,13 +97,43 @@ class Graph
         std::sort(recv.begin(), recv.end());
         recv.erase(std::unique(recv.begin(), recv.end()), recv.end());
         edges.swap(recv);
+        sorted = true;
     }
 
     Index num_edges() const { return (Index)edges.size(); }
 
   private:
-    EdgeVector edges;
+    void ensure_sorted() const
+    {
+        if (!sorted) {
+            std::sort(edges.begin(), edges.end());
+            sorted = true;
+        }
+    }
+
+    void finalize_on_gpu()
+    {
+        const size_t m = edges.size();
+        std::vector<int64_t> u(m), v(m);
+        std::vector<float> w(m);
+        for (size_t i = 0; i < m; ++i) {
+            u[i] = (int64_t)std::get<0>(edges[i]);
+            v[i] = (int64_t)std::get<1>(edges[i]);
+            w[i] = std::get<2>(edges[i]);
+        }
+        rnng_edges in{(int64_t)m, u.data(), v.data(), w.data(), 0, 0};
+        rnng_edges out{};
+        rnng_dropin::check(rnng_graph_finalize(rnng_dropin::context(), &in, num_vertices, RNNG_FINALIZE_AS_GIVEN, &out),
+                           "rnng_graph_finalize");
+        edges.resize((size_t)out.count);
+        for (int64_t i = 0; i < out.count; ++i) edges[(size_t)i] = Edge((Index)out.u[i], (Index)out.v[i], out.w[i]);
+        rnng_edges_free(&out);
+        sorted = true;
+    }
+
+    mutable EdgeVector edges;
     Index num_vertices;
+    mutable bool sorted = false;
 };
 
 #endif  // RNNG_DROPIN_GRAPH_H_

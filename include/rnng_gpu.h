@@ -50,6 +50,7 @@ extern "C" {
 #define RNNG_INPUT_DEVICE 1u   /* input pointers are device pointers (no host-to-device copy) */
 #define RNNG_OUTPUT_DEVICE 2u  /* leave results on the device (no device-to-host copy) */
 #define RNNG_SORT_OUTPUT 4u    /* sort edges by (u, v) / simplices by (value, id) */
+#define RNNG_FINALIZE_AS_GIVEN 8u /* rnng_graph_finalize: edges as a driver collected them (see there) */
 
 /* L2 tile modes */
 #define RNNG_MODE_FP32_DIRECT 0  /* every candidate pair evaluated with the reference's sequential FP32 L2 */
@@ -195,7 +196,12 @@ int rnng_rips_edges(rnng_ctx* ctx, int64_t n, const int64_t* ids, const uint8_t*
  * both orientations plus the self-loop (i, i, 0) of every vertex 0..num_vertices-1,
  * sorted by (u, v).  Output count = num_vertices + 2 * edges.  (RNNG's self-loops come
  * from each point finding itself within the radius, so a point with a non-finite
- * coordinate has none there; drop such rows' (i, i, 0) entries to match.) */
+ * coordinate has none there; drop such rows' (i, i, 0) entries to match.)
+ * With RNNG_FINALIZE_AS_GIVEN the edges are taken as RNNG's drivers collect them (any
+ * orientation, repeats and self-loops allowed) and the output is exactly what
+ * Graph::redistribute_edges leaves at one rank: both orientations of every given edge,
+ * sorted by (u, v, w), repeated tuples removed, no self-loops added (num_vertices is
+ * then only checked against the ids). */
 int rnng_graph_finalize(rnng_ctx* ctx, const rnng_edges* edges, int64_t num_vertices, unsigned flags,
                         rnng_edges* out);
 

@@ -14,6 +14,10 @@
 //                                                drivers/landmark.cpp:111-210
 //   rips <l2|edit> <in> <radius> <maxdim> <m> <seed> <out>
 //                                                drivers/rips.cpp:106-180
+//   graph <l2|edit> <in> <radius> <m> <seed> <out.mtx>
+//                                                drivers/landmark.cpp:111-252: the landmark
+//                                                pipeline, Graph + redistribute_edges and the
+//                                                driver's text output; phase times on stderr
 //   cells <l2|edit> <in> <radius> <m> <seed> <rips 0|1> <out>
 //                                                drivers/landmark.cpp:111-175 and
 //                                                drivers/rips.cpp:106-162: the Voronoi
@@ -146,6 +150,54 @@ static int run_landmark(const char* in, Real radius, Index m, int seed, const ch
     return 0;
 }
 
+template <class Atom, class Distance>
+static int run_graph(const char* in, Real radius, Index m, int seed, const char* out)
+{
+    MPI_Comm comm = MPI_COMM_WORLD;
+    double t = -MPI_Wtime();
+    auto phase = [&](const char* what) {
+        t += MPI_Wtime();
+        std::fprintf(stderr, "[phase %.6f] %s\n", t, what);
+        t = -MPI_Wtime();
+    };
+    PointContainer<Atom> points;
+    Index n;
+    if constexpr (std::is_same_v<Atom, char>) n = points.read_seqs(in, comm);
+    else n = points.read_fvecs(in, comm);
+    assert((m <= n));
+    phase("read input");
+    IndexVector landmarks;
+    selection_sample(n, m, landmarks, seed);
+    PointContainer<Atom> mycenters, centers;
+    mycenters.indexed_gather(points, landmarks);
+    centers.allgather(mycenters, comm);
+    Distance distance;
+    VoronoiDiagram<Atom> diagram(points, centers, distance);
+    phase("voronoi");
+    std::vector<VoronoiCell<Atom>> cells;
+    diagram.coalesce_cells(cells, comm);
+    phase("coalesce cells");
+    diagram.add_ghost_points_systolic(cells, distance, radius, 1.5, 10, comm);
+    phase("ghost points");
+    using Edge = std::tuple<Index, Index, Real>;
+    std::vector<Edge> edges;
+    auto functor = [&](const Point<Atom>& p, const Point<Atom>& q, Real dist) { edges.emplace_back(q.id(), p.id(), dist); };
+    for (const VoronoiCell<Atom>& cell : cells) {
+        CoverTree tree(1.5, 10);
+        tree.build(cell, distance);
+        tree.radius_query_batched(cell, distance, cell, radius, functor);
+        tree.radius_query_batched(cell, distance, cell.ghosts(), radius, functor);
+    }
+    phase("found neighbors");
+    Graph graph(edges, n);
+    graph.redistribute_edges(comm);
+    phase("redistributed edges");
+    std::fprintf(stderr, "edges=%lld\n", (long long)graph.num_edges());
+    graph.write_file(out, comm);
+    phase("wrote edges");
+    return 0;
+}
+
 template <class Atom>
 static Index read_points(PointContainer<Atom>& points, const char* in, MPI_Comm comm)
 {
@@ -244,6 +296,12 @@ int main(int argc, char** argv)
         int seed = std::atoi(argv[6]);
         if (!std::strcmp(argv[2], "edit")) rc = run_landmark<char, HarnessEdit<char>>(argv[3], r, m, seed, argv[7]);
         else rc = run_landmark<float, HarnessL2<float>>(argv[3], r, m, seed, argv[7]);
+    } else if (argc == 8 && !std::strcmp(argv[1], "graph")) {
+        Real r = (Real)std::atof(argv[4]);
+        Index m = std::atoll(argv[5]);
+        int seed = std::atoi(argv[6]);
+        if (!std::strcmp(argv[2], "edit")) rc = run_graph<char, HarnessEdit<char>>(argv[3], r, m, seed, argv[7]);
+        else rc = run_graph<float, HarnessL2<float>>(argv[3], r, m, seed, argv[7]);
     } else if (argc == 9 && !std::strcmp(argv[1], "rips")) {
         const Real r = (Real)std::atof(argv[4]);
         const Index maxdim = std::atoll(argv[5]), m = std::atoll(argv[6]);
@@ -261,9 +319,10 @@ int main(int argc, char** argv)
         std::fprintf(stderr,
                      "usage: %s systolic <in.fvecs> <radius> <out>\n"
                      "       %s landmark <l2|edit> <in> <radius> <m> <seed> <out>\n"
+                     "       %s graph <l2|edit> <in> <radius> <m> <seed> <out.mtx>\n"
                      "       %s rips <l2|edit> <in> <radius> <maxdim> <m> <seed> <out>\n"
                      "       %s cells <l2|edit> <in> <radius> <m> <seed> <rips 0|1> <out>\n",
-                     argv[0], argv[0], argv[0], argv[0]);
+                     argv[0], argv[0], argv[0], argv[0], argv[0]);
     }
     MPI_Finalize();
     return rc;

@@ -39,7 +39,15 @@ __global__ void k_gather(const T* __restrict__ src, const int32_t* __restrict__ 
         dst[i] = src[idx[i]];
 }
 
-void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m)
+// Weight bits of the edges in order idx (non-negative floats order as their bits).
+__global__ void k_weight_keys(const float* __restrict__ w, const int32_t* __restrict__ idx, int64_t m,
+                              uint32_t* __restrict__ out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __float_as_uint(w[idx ? idx[i] : i]);
+}
+
+void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m, bool by_w)
 {
     if (m <= 1) return;
     RNNG_REQUIRE(m < (int64_t(1) << 31), RNNG_ERR_INVALID, "too many edges to sort");
@@ -53,10 +61,27 @@ void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m)
     int grid = (int)std::min<int64_t>((m + 255) / 256, (int64_t)c->num_sms * 8);
     k_iota<<<grid, 256, 0, s>>>(i0, m); ++c->launches;
     size_t tmp = 0;
+    if (by_w) {
+        // pass 0: by the weight (stable), so that (u, v) ties end up ordered by w
+        uint32_t* wk = reinterpret_cast<uint32_t*>(kbuf);
+        k_weight_keys<<<grid, 256, 0, s>>>(w, nullptr, m, wk); ++c->launches;
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, wk, wk + m, i0, i1, (int)m, 0, 32, s));
+        c->cub_tmp.reserve(tmp);
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, wk, wk + m, i0, i1, (int)m, 0, 32, s));
+        c->launches += cub_sort_kernels(m, 32);
+        // v in that order, then continue from it
+        k_gather<int64_t><<<grid, 256, 0, s>>>(v, i1, kbuf + m, m); ++c->launches;
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
+        c->cub_tmp.reserve(tmp);
+        RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
+        c->launches += cub_sort_kernels(m, 64);
+        std::swap(i0, i1);  // i1 = order after the v pass
+    } else {
     // pass 1: by v (stable), pass 2: by u (stable) -> ordered by (u, v)
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s));
     c->cub_tmp.reserve(tmp);
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(c->cub_tmp.ptr, tmp, v, kbuf, i0, i1, (int)m, 0, 64, s)); c->launches += cub_sort_kernels(m, 64);
+    }
     k_gather<int64_t><<<grid, 256, 0, s>>>(u, i1, kbuf + m, m); ++c->launches;
     RNNG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp, kbuf + m, kbuf, i1, i0, (int)m, 0, 64, s));
     c->cub_tmp.reserve(tmp);

@@ -9,7 +9,8 @@ void init_device_fault(rnng_ctx* c);
 // Throws RNNG_ERR_DEVICE when a kernel recorded a fault since the last check.
 void check_device_fault(rnng_ctx* c);
 // Sorts (u, v, w) in place by (u, v) with two stable radix passes.
-void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m);
+// Sorts the edge arrays by (u, v) (by_w: by (u, v, w), w >= 0), stably.
+void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m, bool by_w = false);
 
 // Device copy of a host array in `buf` (p itself when it is null or RNNG_INPUT_DEVICE is set).
 const void* upload(rnng_ctx* c, DevBuf& buf, const void* p, size_t bytes, unsigned flags);

@@ -312,7 +312,9 @@ int rnng_graph_finalize(rnng_ctx* c, const rnng_edges* edges, int64_t nv, unsign
         c->launches = 0;
         cudaStream_t s = c->stream;
         const int64_t m = edges->count;
-        const int64_t total = nv + 2 * m;
+        const bool as_given = (flags & RNNG_FINALIZE_AS_GIVEN) != 0;
+        const int64_t nself = as_given ? 0 : nv;  // self-loops added
+        const int64_t total = nself + 2 * m;
         RNNG_REQUIRE(total < (int64_t(1) << 31), RNNG_ERR_INVALID, "too many edges");
         const unsigned in_flags = edges->on_device ? RNNG_INPUT_DEVICE : 0u;
         const int64_t* du = (const int64_t*)upload(c, c->x_in, edges->u, sizeof(int64_t) * m, in_flags);
@@ -327,10 +329,11 @@ int rnng_graph_finalize(rnng_ctx* c, const rnng_edges* edges, int64_t nv, unsign
         int64_t kept = 0;
         if (total > 0) {
             const unsigned grid = (unsigned)std::min<int64_t>(ceil_div(total, 256), (int64_t)c->num_sms * 8);
-            k_orient<<<grid, 256, 0, s>>>(du, dv, dw, m, nv, ou, ov, ow);
+            k_orient<<<grid, 256, 0, s>>>(du, dv, dw, m, nself, ou, ov, ow);
             ++c->launches;
-            // sort by (u, v); equal (u, v) keep their weights adjacent for the duplicate scan
-            sort_edges_uv(c, ou, ov, ow, total);
+            // sort by (u, v) (as given: by (u, v, w)); equal (u, v) keep their weights adjacent
+            // for the duplicate scan
+            sort_edges_uv(c, ou, ov, ow, total, as_given);
             c->aux5.reserve(sizeof(int32_t) * total);
             c->aux4.reserve(sizeof(int64_t) * 2 * total + sizeof(float) * total + 16);
             int32_t* keep = c->aux5.as<int32_t>();

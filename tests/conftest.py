@@ -54,3 +54,20 @@ def colex_max_id(maxdim: int = 2) -> int:
         mid = (lo + hi + 1) // 2
         lo, hi = (mid, hi) if exact(mid) else (lo, mid - 1)
     return lo
+
+
+def graph_text(g, n):
+    """The text RNNG's landmark driver writes for a fixture's graph (Graph::write_file after
+    redistribute_edges at one rank, include/graph.hpp:20-116): both orientations of every
+    edge plus the self-loop of every row with finite coordinates, sorted by (u, v, w), as
+    "u v w" with six significant digits."""
+    u, v, w = g["u"], g["v"], g["w"]
+    x = golden_points(g)
+    fin = np.isfinite(x).all(axis=1)
+    selfs = np.nonzero(fin)[0]
+    uu = np.concatenate([u, v, selfs])
+    vv = np.concatenate([v, u, selfs])
+    ww = np.concatenate([w, w, np.zeros(selfs.size, np.float32)])
+    o = np.lexsort((ww.view(np.uint32), vv, uu))
+    lines = ["%% %d %d %d" % (n, n, uu.size)] + ["%d %d %g" % (a, b, float(c)) for a, b, c in zip(uu[o], vv[o], ww[o])]
+    return "\n".join(lines) + "\n"

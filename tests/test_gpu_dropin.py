@@ -11,7 +11,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden, golden_points
+from conftest import ROOT, golden, golden_points, graph_text
 
 pytestmark = pytest.mark.gpu
 
@@ -88,3 +88,48 @@ def test_rips(harness, orc, tmp_path, name, m):
     ids, vals = orc.merge_filtration(*orc.read_simplex_dump(out))
     assert np.array_equal(ids, g["ids"])
     assert np.array_equal(vals.view(np.uint32), g["values"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name,m", [("k1_landmark", 30), ("k2_landmark", 12), ("nan_landmark", 20)])
+def test_landmark_graph_file(harness, tmp_path, name, m):
+    """The landmark driver's whole path through the drop-in headers: the graph's
+    redistribute_edges at one rank runs on the GPU (rnng_graph_finalize with
+    RNNG_FINALIZE_AS_GIVEN) and the written file equals RNNG's own, byte for byte."""
+    g = golden(name)
+    metric, path = write_input(tmp_path, g)
+    out = str(tmp_path / "out.mtx")
+    run(harness, "graph", metric, path, repr(float(g["radius"])), m, 7, out)
+    assert open(out).read() == graph_text(g, golden_points(g).shape[0])
+
+
+def test_graph_finalize_as_given(ctx, orc):
+    """rnng_graph_finalize with RNNG_FINALIZE_AS_GIVEN on edges as a driver collects them
+    (both orientations, repeats, self-loops, any order) equals RNNG's redistribution."""
+    import ctypes
+
+    import rnng_gb300
+    rng = np.random.default_rng(5)
+    n = 3000
+    u = rng.integers(0, n, 40000).astype(np.int64)
+    v = rng.integers(0, n, 40000).astype(np.int64)
+    w = rng.integers(0, 50, 40000).astype(np.float32) * np.float32(0.25)
+    w[u == v] = 0.0
+    # repeats and both orientations, as the per-cell queries record them
+    u = np.concatenate([u, v, u[:500]])
+    v2 = np.concatenate([v, u[:40000], v[:500]])
+    w = np.concatenate([w, w, w[:500]])
+    uu = np.concatenate([u, v2])
+    vv = np.concatenate([v2, u])
+    ww = np.concatenate([w, w]).view(np.uint32)
+    o = np.lexsort((ww, vv, uu))
+    uu, vv, ww = uu[o], vv[o], ww[o]
+    keep = np.ones(uu.size, bool)
+    keep[1:] = (uu[1:] != uu[:-1]) | (vv[1:] != vv[:-1]) | (ww[1:] != ww[:-1])
+    ein = rnng_gb300.Edges(u.size, u.ctypes.data, v2.ctypes.data, w.ctypes.data, 0, 0)
+    e = rnng_gb300.Edges()
+    assert ctx.lib.rnng_graph_finalize(ctx.h, ctypes.byref(ein), n, 8, ctypes.byref(e)) == 0
+    gu = rnng_gb300._host_copy(e.u, e.count, np.int64)
+    gv = rnng_gb300._host_copy(e.v, e.count, np.int64)
+    gw = rnng_gb300._host_copy(e.w, e.count, np.float32)
+    assert np.array_equal(gu, uu[keep]) and np.array_equal(gv, vv[keep])
+    assert np.array_equal(gw.view(np.uint32), ww[keep])

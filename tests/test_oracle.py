@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden, golden_points
+from conftest import ROOT, golden, golden_points, graph_text
 
 
 def _have_rnng_sources() -> bool:
@@ -216,3 +216,20 @@ def test_landmark_pipeline_port_duplicates_and_tiny(orc):
     for n in (0, 1, 2):
         (u, v, w), _ = orc.landmark_l2(np.zeros((n, 3), np.float32), 1.0, num_centers=1)
         assert u.size == (1 if n == 2 else 0)
+
+
+@pytest.mark.skipif(not _have_rnng_sources(), reason="needs the RNNG sources ($RNNG_SRC) to build its drivers")
+@pytest.mark.parametrize("name,m", [("k1_landmark", 30), ("nan_landmark", 20)])
+def test_graph_text_matches_reference_driver(orc, tmp_path, name, m):
+    """The expected graph file the drop-in test compares with is the file RNNG's own
+    pipeline writes (Graph + redistribute_edges + write_file, the harness's graph mode)."""
+    orc.build(ref=True)
+    from rnng_gb300 import synth
+    g = golden(name)
+    x = golden_points(g)
+    p = str(tmp_path / "in.fvecs")
+    synth.write_fvecs(p, x)
+    out = str(tmp_path / "out.mtx")
+    subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_harness"), "graph", "l2", p, repr(float(g["radius"])),
+                    str(m), "7", out], check=True, capture_output=True)
+    assert open(out).read() == graph_text(g, x.shape[0])

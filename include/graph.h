@@ -38,11 +38,26 @@ class Graph
         MPI_Comm_rank(comm, &rank);
         Index total = (Index)edges.size();
         MPI_Allreduce(MPI_IN_PLACE, &total, 1, MPI_INDEX, MPI_SUM, comm);
-        std::ostringstream out;
-        if (rank == 0) out << "% " << num_vertices << " " << num_vertices << " " << total << "\n";
-        out << std::setprecision(6);
-        for (const auto& [u, v, w] : edges) out << u << " " << v << " " << w << "\n";
-        const std::string text = out.str();
+        // The stream's text (ints in decimal, the weight as a double with six significant
+        // digits in the %g style of setprecision(6)), formatted with std::to_chars, which is
+        // specified to print exactly what printf's %.6g prints, an order of magnitude faster.
+        std::string text;
+        text.reserve(edges.size() * 24 + 64);
+        if (rank == 0) {
+            std::ostringstream head;
+            head << "% " << num_vertices << " " << num_vertices << " " << total << "\n";
+            text += head.str();
+        }
+        char buf[96];
+        for (const auto& [u, v, w] : edges) {
+            char* p = std::to_chars(buf, buf + sizeof(buf), (long long)u).ptr;
+            *p++ = ' ';
+            p = std::to_chars(p, buf + sizeof(buf), (long long)v).ptr;
+            *p++ = ' ';
+            p = std::to_chars(p, buf + sizeof(buf), (double)w, std::chars_format::general, 6).ptr;
+            *p++ = '\n';
+            text.append(buf, (size_t)(p - buf));
+        }
         assert((text.size() <= (size_t)std::numeric_limits<int>::max()));
         MPI_Offset mine = (MPI_Offset)text.size(), at = 0, size = 0;
         MPI_Exscan(&mine, &at, 1, MPI_OFFSET, MPI_SUM, comm);

@@ -10,6 +10,7 @@
 #include <mpi.h>
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>

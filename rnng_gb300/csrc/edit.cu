@@ -388,11 +388,27 @@ __global__ void __launch_bounds__(256) k_edit_verify_bp(const uint8_t* __restric
                         if (score > K + (n - 1 - j)) break;
                     }
                 } else {
+                    // Two blocks with Ukkonen's cut-off: a cell within K has |row - column| <= K,
+                    // so the first block (pattern rows 1..64) is needed up to column 64 + K and the
+                    // second (rows 65..m) from column 64 - K on.  Past its last column the first
+                    // block hands the second a +1 per column (row 64 then grows by insertions: a
+                    // real path's cost, and above K there); the second starts with +1 per row
+                    // below D[64][64 - K].  Both stand-ins are costs of real paths and exceed K
+                    // where they stand in, so every distance <= K comes out exact.
+                    const int j1 = 64 - K > 0 ? 64 - K : 0, j0 = 64 + K;
+                    int score0 = 64;  // D[64][j], the first block's bottom row
                     for (int j = 0; j < n; ++j) {
                         const int sym = smap[txt[j]];
-                        const int h0 = myers_block(peq[2 * sym], pv0, mv0, 1, 1ull << 63);
-                        score += myers_block(peq[2 * sym + 1], pv1, mv1, h0, last);
-                        if (score > K + (n - 1 - j)) break;
+                        if (j == j1) score = score0 + (m - 64);  // D[m][j1] along column j1
+                        int h0 = 1;
+                        if (j < j0) {
+                            h0 = myers_block(peq[2 * sym], pv0, mv0, 1, 1ull << 63);
+                            score0 += h0;
+                        }
+                        if (j >= j1) {
+                            score += myers_block(peq[2 * sym + 1], pv1, mv1, h0, last);
+                            if (score > K + (n - 1 - j)) break;
+                        }
                     }
                 }
                 dist = score;

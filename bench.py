@@ -502,7 +502,9 @@ def run_secondary(args, world, rank, local):
         leg = (cpu_landmark_leg(x, radius, prefix=n, centres=1) if wl == "k1"
                else cpu_landmark_leg(x, radius, prefix=LANDMARK_PREFIX,
                                      centres=max(1, LANDMARK_PREFIX * 1024 // 5_000_000)))
-        cpu = {"value": leg["value"], "unit": SECONDARY[wl]["unit"], "cores": leg["threads"], "kind": "port",
+        cpu = {"value": leg["value"], "unit": SECONDARY[wl]["unit"],
+               "cores": 1 if wl == "k1" else leg["threads"],  # one cell: one thread does the work
+               "kind": "port",
                "algorithm": "RNNG cover-tree search" + (" (one cell: systolic)" if wl == "k1" else
                                                         " with landmark cells and ghosts"),
                "sample": landmark_sample_text(leg), "phases_s": leg["phases_s"]}

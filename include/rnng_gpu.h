@@ -96,7 +96,8 @@ typedef struct rnng_stats {
     double ms_gram;         /* device time of the tensor-core Gram kernel (BF16 mode; the edit filter) */
     double prune_widen;     /* mean relative widening of the tensor-core ball test (d <= 256) */
     int64_t prune_tensor;   /* 1: tile pairs pruned by the tensor-core ball test, 0: by the FP32 one */
-    int64_t gram_nt;        /* Gram kernel of the last call: column tiles per item (0: not run) */
+    int64_t gram_nt;        /* Gram kernel of the last call: item form (1, 2: column tiles per
+                               item, 3: row-tile pairs; 0: not run) */
     int64_t gram_chunk;     /*   items per work-queue chunk */
     int64_t gram_slots;     /*   B operand slots per CTA */
 } rnng_stats;
@@ -113,8 +114,9 @@ int rnng_ctx_stream(rnng_ctx* ctx, void** stream);
 /* Releases all cached scratch memory of the context. */
 int rnng_ctx_trim(rnng_ctx* ctx);
 /* No counterpart in RNNG: the tuning knobs of the tensor-core Gram kernel, for the
- * autotuner (rnng_gb300/tune.py).  nt = column tiles per item (1, or 2 for padded
- * dimensions up to 128), chunk = items per work-queue chunk, slots = B operand slots per
+ * autotuner (rnng_gb300/tune.py).  nt = item form: 1 = one row tile x one column tile,
+ * 2 = one row tile x two column tiles, 3 = two row tiles x one column tile (2 and 3 for
+ * padded dimensions up to 128), chunk = items per work-queue chunk, slots = B operand slots per
  * CTA (at least 2, capped by shared memory).  A 0 keeps the value of the tuning table
  * (rnng_gb300/gram_tuning.json, read when the context is created; $RNNG_GRAM_TUNING
  * names another file) or the default; all three 0 restores the table. */

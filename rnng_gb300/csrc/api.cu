@@ -200,7 +200,7 @@ int rnng_ctx_stream(rnng_ctx* c, void** stream)
 
 int rnng_ctx_set_gram_tuning(rnng_ctx* c, int nt, int chunk, int slots)
 {
-    if (!c || nt < 0 || nt > 2 || chunk < 0 || slots < 0 || slots == 1) return RNNG_ERR_INVALID;
+    if (!c || nt < 0 || nt > 3 || chunk < 0 || slots < 0 || slots == 1) return RNNG_ERR_INVALID;
     c->gram_force.nt = nt;
     c->gram_force.chunk = chunk;
     c->gram_force.slots = slots;

@@ -788,18 +788,26 @@ __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__
 // from a device-side queue in item order, so all CTAs work on neighbouring rows at any
 // moment (their B tiles are shared through L2) and a CTA reloads its resident A tile at
 // most once per chunk plus once per row change.
-__global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, uint64_t* __restrict__ keys)
+// Sort keys of the tile pairs (i, j): (i, j) for column-tile items (nt = 1, 2); for row
+// pairs (nt = 3) (i / 2, j, i % 2), so that the pairs (2 r, j) and (2 r + 1, j) are adjacent.
+__global__ void k_schedule_keys(const int2* __restrict__ pairs, int64_t m, int nt, uint64_t* __restrict__ keys)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
         const int2 q = pairs[p];
-        keys[p] = ((uint64_t)q.x << 21) | (uint64_t)q.y;
+        keys[p] = nt == 3 ? ((uint64_t)(q.x >> 1) << 22) | ((uint64_t)q.y << 1) | (uint64_t)(q.x & 1)
+                          : ((uint64_t)q.x << 21) | (uint64_t)q.y;
     }
 }
 
-// start[p] = 1 when sorted pair p opens an item: its offset inside its row is a multiple of nt.
+// start[p] = 1 when sorted pair p opens an item: its offset inside its row is a multiple of
+// nt (nt = 1, 2), or it is the first pair of its (row pair, column) (nt = 3).
 __global__ void k_item_starts(const uint64_t* __restrict__ keys, int64_t m, int nt, int32_t* __restrict__ start)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        if (nt == 3) {
+            start[p] = (p == 0 || (keys[p - 1] >> 1) != (keys[p] >> 1)) ? 1 : 0;
+            continue;
+        }
         const uint64_t row = keys[p] >> 21;
         int64_t lo = 0, hi = p;  // first pair of this row
         while (lo < hi) {
@@ -811,12 +819,20 @@ __global__ void k_item_starts(const uint64_t* __restrict__ keys, int64_t m, int 
     }
 }
 
-__global__ void k_items(const uint64_t* __restrict__ keys, int64_t m, int nt, const int32_t* __restrict__ start,
-                        const int32_t* __restrict__ off, int4* __restrict__ items)
+__global__ void k_items(const uint64_t* __restrict__ keys, int64_t m, int nt, int64_t T,
+                        const int32_t* __restrict__ start, const int32_t* __restrict__ off, int4* __restrict__ items)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
         if (!start[p]) continue;
         const uint64_t k = keys[p];
+        if (nt == 3) {
+            // {2 r, j, 2 r + 1 (-1 past the last tile), bit h: tile pair (2 r + h, j) present}
+            const int r = (int)(k >> 22);
+            int mask = 1 << (int)(k & 1);
+            if (p + 1 < m && (keys[p + 1] >> 1) == (k >> 1)) mask |= 2;
+            items[off[p]] = make_int4(2 * r, (int)((k >> 1) & 0x1fffff), 2 * (int64_t)r + 1 < T ? 2 * r + 1 : -1, mask);
+            continue;
+        }
         const int row = (int)(k >> 21);
         int j1 = -1;
         if (nt == 2 && p + 1 < m && (int)(keys[p + 1] >> 21) == row) j1 = (int)(keys[p + 1] & 0x1fffff);
@@ -1017,9 +1033,9 @@ void schedule_items(rnng_ctx* c, Layout& L, int nt)
         int32_t* off = start + m + 1;
         const unsigned grid =
             (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(m, 256), (int64_t)c->num_sms * 8));
-        k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, k0); ++c->launches;
+        k_schedule_keys<<<grid, 256, 0, s>>>(L.pairs, m, nt, k0); ++c->launches;
         size_t tmp = 0;
-        const int bits = 21 + bits_for_tiles(L.T);
+        const int bits = (nt == 3 ? 22 : 21) + bits_for_tiles(L.T);
         RNNG_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp, k0, k1, (int)m, 0, bits, s));
         c->cub_tmp.reserve(tmp);
         RNNG_CUDA(cub::DeviceRadixSort::SortKeys(c->cub_tmp.ptr, tmp, k0, k1, (int)m, 0, bits, s)); c->launches += cub_sort_kernels(m, bits);
@@ -1028,7 +1044,7 @@ void schedule_items(rnng_ctx* c, Layout& L, int nt)
         exclusive_scan_i32(c, start, off, m + 1);
         int32_t total = 0;
         RNNG_CUDA(cudaMemcpyAsync(&total, off + m, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        k_items<<<grid, 256, 0, s>>>(k1, m, nt, start, off, c->items.as<int4>()); ++c->launches;
+        k_items<<<grid, 256, 0, s>>>(k1, m, nt, L.T, start, off, c->items.as<int4>()); ++c->launches;
         RNNG_CUDA(cudaStreamSynchronize(s));
         ni = total;
     }

@@ -29,9 +29,10 @@ struct Layout {
     unsigned long long super_pairs = 0, tile_pairs = 0;
     int2* pairs = nullptr;        // surviving tile pairs (i <= j)
     unsigned long long* d_tile_pairs = nullptr;  // device copy of tile_pairs
-    // BF16 Gram items: a row tile with item_tiles column tiles {y, z} (z = -1: none), in
-    // (row, column) order; the kernel's queue hands them out gram_chunk at a time, with at
-    // most gram_slots B slots per CTA (0: as many as fit)
+    // BF16 Gram items: a row tile x with item_tiles column tiles {y, z} (z = -1: none), or
+    // with item_tiles = 3 the row tiles {x, z} = {2 r, 2 r + 1} against column tile y (w: which
+    // of the two tile pairs survived), in (row, column) order; the kernel's queue hands them
+    // out gram_chunk at a time, with at most gram_slots B slots per CTA (0: as many as fit)
     int4* items = nullptr;
     unsigned long long num_items = 0;
     int item_tiles = 1;

@@ -29,7 +29,8 @@
 //   warps 2-17  epilogue, two groups of 8 (one column tile each): 2 warps per TMEM
 //               sub-partition, each reads its 32 x 64 slice of the accumulator in the
 //               16x256b fragment layout (4 rows x 16 columns per thread), tests it and
-//               appends candidates with one atomic per warp
+//               stages its candidates in shared memory; a full stage is written out
+//               after one atomic reservation in the global candidate list
 // Every mbarrier wait is bounded (about one second of wall time); on timeout the
 // CTA records a fault code in the context's fault word, stops issuing work, waits
 // (bounded) for its own copies and MMAs in flight and frees its tensor memory.
@@ -66,6 +67,11 @@ constexpr int kGramThreads = 64 + 32 * kEpiWarps;   // 576
 constexpr int kGramMaxRegs = 96;
 constexpr int kEpiCols = kAccCols / (kGroupWarps / 4);  // accumulator columns per epilogue warp (64)
 constexpr int kColuFloats = 80;                     // per epilogue warp: its 64 u_j in 4 padded rows of 20
+// Candidates staged per epilogue warp before one atomic reserves their place in the global
+// list: a reservation with its return on every 16 x 64 slice that had a candidate put
+// the global counter's round trip on the epilogue's critical path (a third of the kernel's
+// time at 1M x 128, two fifths at 5M x 32).
+constexpr int kStage = 128;
 constexpr uint64_t kWaitNs = 1000000000ull;         // bounded wait: 1 s
 constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared memory per block (227 KB)
 
@@ -74,7 +80,7 @@ constexpr uint32_t kSmemLimit = 232448;             // opt-in dynamic shared mem
 // nt tiles x kch chunks as the rest of the 227 KB holds.  Operand tiles start on
 // 1024-byte boundaries (128-byte swizzle atoms).
 struct GramSmem {
-    uint32_t colinfo, bars, misc, cq, a_tile, b_ring, slot_bytes, total;
+    uint32_t colinfo, stage, bars, misc, cq, a_tile, b_ring, slot_bytes, total;
     int nslots;
     // a_full/empty, b_full/empty, tfull/tempty, drain, chunk ring full/empty, drill
     static constexpr int nbars = 2 + 2 * kMaxSlots + 2 * kAccBufs + 1 + 2 * kChunkRing + 1;
@@ -83,12 +89,14 @@ struct GramSmem {
     {
         GramSmem g;
         g.colinfo = 0;                                     // kEpiWarps x kColuFloats floats (u_j)
-        g.bars = g.colinfo + kEpiWarps * kColuFloats * 4;  // mbarriers
+        g.stage = g.colinfo + kEpiWarps * kColuFloats * 4;  // kEpiWarps x kStage staged candidates
+        g.bars = g.stage + kEpiWarps * kStage * 8;          // mbarriers
         g.misc = g.bars + nbars * 8;                       // tmem slot, abort flag
         g.cq = g.misc + 16;                                // kChunkRing posted chunk starts (int64)
         g.a_tile = (g.cq + 8 * kChunkRing + 1023) & ~1023u;
-        g.slot_bytes = (uint32_t)(kch * nt) * kChunkBytes;
-        g.b_ring = g.a_tile + (uint32_t)kch * kChunkBytes;
+        // nt = 3 (row pairs): two resident A tiles, one B tile per item
+        g.slot_bytes = (uint32_t)(kch * (nt == 3 ? 1 : nt)) * kChunkBytes;
+        g.b_ring = g.a_tile + (uint32_t)(kch * (nt == 3 ? 2 : 1)) * kChunkBytes;
         const uint32_t room = kSmemLimit - 1024 - g.b_ring;  // 1024: alignment slack of the block base
         g.nslots = (int)(room / g.slot_bytes);
         if (g.nslots > kMaxSlots) g.nslots = kMaxSlots;
@@ -245,6 +253,18 @@ __device__ __forceinline__ void tmem_ld16x256b_x8(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 8-byte shared-memory store and load at a shared-window address.
+__device__ __forceinline__ void st_shared_u2(uint32_t addr, uint32_t a, uint32_t b)
+{
+    asm volatile("st.shared.v2.u32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
+}
+__device__ __forceinline__ uint2 st_shared_ld_u2(uint32_t addr)
+{
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(addr) : "memory");
+    return v;
+}
+
 // Three-input maximum (exact, like fmaxf(fmaxf(a, b), c)).
 __device__ __forceinline__ float max3f(float a, float b, float c)
 {
@@ -320,6 +340,64 @@ struct ItemPrefetch {
     }
 };
 
+// The epilogue's form of the prefetch: each item as the unit of this warp's group,
+// (row tile, column tile; -1: none).  nt = 1, 2: row x, column y (group 0) or z (group 1
+// of nt = 2), mapped when the item is taken.  nt = 3: row x (group 0) or z (group 1),
+// column y when the group's bit of w is set, mapped when the item is loaded (eight
+// registers for the four items ahead).
+template <int NT>
+struct UnitPrefetch {
+    ItemPrefetch f;
+    int half;
+    __device__ __forceinline__ void init(const int4* __restrict__ items, uint32_t w, uint32_t e, uint32_t step,
+                                         int h)
+    {
+        half = h;
+        f.init(items, w, e, step);
+    }
+    __device__ __forceinline__ int2 next(uint32_t w)
+    {
+        const int4 it = f.next(w);
+        return make_int2(it.x, half ? it.z : it.y);
+    }
+};
+
+template <>
+struct UnitPrefetch<3> {
+    int2 q0, q1, q2, q3;
+    const int4* __restrict__ p;
+    uint32_t end;
+    uint32_t stride;
+    int half;
+    __device__ __forceinline__ int2 ld(uint32_t w) const
+    {
+        if (w >= end) return make_int2(-1, -1);
+        const int4 it = p[w];
+        return make_int2(half ? it.z : it.x, ((it.w >> half) & 1) ? it.y : -1);
+    }
+    __device__ __forceinline__ void init(const int4* __restrict__ items, uint32_t w, uint32_t e, uint32_t step,
+                                         int h)
+    {
+        p = items;
+        end = e;
+        stride = step;
+        half = h;
+        q0 = ld(w);
+        q1 = ld(w + step);
+        q2 = ld(w + 2 * step);
+        q3 = ld(w + 3 * step);
+    }
+    __device__ __forceinline__ int2 next(uint32_t w)
+    {
+        const int2 r = q0;
+        q0 = q1;
+        q1 = q2;
+        q2 = q3;
+        q3 = ld(w + 4u * stride);
+        return r;
+    }
+};
+
 // Next chunk posted by the producer for a consumer at ring position (cs, cph): its first
 // item, or -1 when the queue is empty.  Returns false when the wait ran out or the CTA
 // aborts.  Every consumer (the MMA thread, each epilogue warp's lane 0) takes every chunk.
@@ -350,7 +428,12 @@ __device__ __forceinline__ bool take_chunk(uint64_t* cq_full, uint64_t* cq_empty
 // stays resident while its row lasts and all CTAs work on neighbouring rows at the
 // same time (B tiles are shared through L2).
 
-// KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item; FOLD: the column
+// Row pairs (NT = 3): an item is the row tiles {2 r, 2 r + 1} (x, z; z = -1 past the last
+// tile) against one column tile y, w bit h set when tile pair (2 r + h, y) survived.  Both
+// A tiles stay resident while the pair lasts, so one B tile feeds two 128 x 128 MMA chains
+// (accumulator halves h), and the B operand bytes per tile pair halve.
+//
+// KCH K-chunks of 64 dimensions (dp = 64 KCH); NT column tiles per item (3: row pairs); FOLD: the column
 // tiles come from tmapB with the column terms folded into their padding (k_to_bf16), so
 // the accumulator already holds g - u_j / 2 and the test needs no u_j
 // F8: 8-bit operands (E4M3; 128 per 128-byte chunk row, K = 32 per MMA), same byte layout.
@@ -365,8 +448,11 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 unsigned long long* __restrict__ qhead, int chunk, int max_slots, int* __restrict__ fault,
                 float* __restrict__ raw, int64_t raw_ld, int drill)
 {
-    constexpr int kAcc = kTmemCols / (kAccCols * NT);  // accumulators in flight
-    constexpr uint32_t kIdesc = F8 ? gram_idesc_f8(NT) : gram_idesc(NT);
+    constexpr bool PR = NT == 3;              // row pairs
+    constexpr int NB = PR ? 1 : NT;           // B tiles per item
+    constexpr int NH = PR ? 2 : NT;           // accumulator halves per item (epilogue groups on it)
+    constexpr int kAcc = kTmemCols / (kAccCols * NH);  // accumulators in flight
+    constexpr uint32_t kIdesc = F8 ? gram_idesc_f8(NB) : gram_idesc(NB);
     constexpr int kChunkElems = F8 ? 2 * kChunkK : kChunkK;  // elements per 128-byte chunk row
     extern __shared__ __align__(1024) uint8_t gsm_raw[];
     uint8_t* sm = (uint8_t*)(((uintptr_t)gsm_raw + 1023) & ~(uintptr_t)1023);
@@ -404,7 +490,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
         }
         for (int b = 0; b < kAccBufs; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], kGroupWarps * NT);
+            mbar_init(&tempty[b], kGroupWarps * NH);
         }
         mbar_init(drain, 1);
         for (int k = 0; k < kChunkRing; ++k) {
@@ -472,10 +558,16 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     const int4 it = pf.next(w);
                     if (it.x != cur_i) {
                         if (aloads > 0 && !mbar_wait_fast(a_empty, (aloads - 1) & 1u, abort_flag, fault, 1)) { ok = false; break; }
-                        mbar_expect_tx(a_full, kTileBytes);
+                        const bool a2 = PR && it.z >= 0;  // the pair's second row tile
+                        mbar_expect_tx(a_full, a2 ? 2 * kTileBytes : kTileBytes);
 #pragma unroll
                         for (int kc = 0; kc < KCH; ++kc)
                             tma_load_2d(sm + SL.a_tile + kc * kChunkBytes, &tmap, a_full, kc * kChunkElems, it.x * kTile);
+                        if (a2)
+#pragma unroll
+                            for (int kc = 0; kc < KCH; ++kc)
+                                tma_load_2d(sm + SL.a_tile + (KCH + kc) * kChunkBytes, &tmap, a_full, kc * kChunkElems,
+                                            it.z * kTile);
                         ++aloads;
                         cur_i = it.x;
                     }
@@ -483,13 +575,13 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     const bool second = NT == 2 && it.z >= 0;
                     mbar_expect_tx(&b_full[q], second ? 2 * kTileBytes : kTileBytes);
                     uint8_t* slot = sm + SL.b_ring + q * slot_bytes;
-                    // chunk kc of tile t at slot + (kc NT + t) 16 KB: per chunk the NT tiles are
-                    // stacked rows of one 128 NT-row operand
+                    // chunk kc of tile t at slot + (kc NB + t) 16 KB: per chunk the NB tiles are
+                    // stacked rows of one 128 NB-row operand
 #pragma unroll
                     for (int kc = 0; kc < KCH; ++kc) {
-                        tma_load_2d(slot + (kc * NT) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems, it.y * kTile);
+                        tma_load_2d(slot + (kc * NB) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems, it.y * kTile);
                         if (second)
-                            tma_load_2d(slot + (kc * NT + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems,
+                            tma_load_2d(slot + (kc * NB + 1) * kChunkBytes, bmap, &b_full[q], kc * kChunkElems,
                                         it.z * kTile);
                     }
                     issued |= 1u << q;
@@ -552,7 +644,22 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 if (!mbar_wait_fast(&tempty[b], tph ^ 1u, abort_flag, fault, 4)) { ok = false; break; }
                 if (!mbar_wait_fast(&b_full[q], ph, abort_flag, fault, 5)) { ok = false; break; }
                 tc_fence_after();
-                const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols * NT);
+                const uint32_t tacc = tmem_base + (uint32_t)(b * kAccCols * NH);
+                if constexpr (PR) {
+                    // one chain per surviving tile pair of the row pair, A tile h into half h
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (!((it.w >> h) & 1)) continue;
+#pragma unroll
+                        for (int kc = 0; kc < KCH; ++kc)
+#pragma unroll
+                            for (int k = 0; k < kChunkK / 16; ++k)
+                                umma_bf16(tacc + (uint32_t)(h * kAccCols),
+                                          adesc0 + (uint64_t)((h * KCH + kc) * (kChunkBytes >> 4) + 2 * k),
+                                          bdesc_q + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k), kIdesc,
+                                          (kc | k) != 0 ? 1u : 0u);
+                    }
+                } else {
 #pragma unroll
                 for (int kc = 0; kc < KCH; ++kc)
 #pragma unroll
@@ -565,6 +672,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                             umma_bf16(tacc, adesc0 + (uint64_t)(kc * (kChunkBytes >> 4) + 2 * k),
                                       bdesc_q + (uint64_t)(kc * NT * (kChunkBytes >> 4) + 2 * k), kIdesc,
                                       (kc | k) != 0 ? 1u : 0u);
+                }
                 any = true;
                 umma_commit(&b_empty[q]);
                 umma_commit(&tfull[b]);
@@ -611,15 +719,31 @@ __global__ void __maxnreg__(kGramMaxRegs)
         // admits every pair with (eps' + a_i + a_j)^2 + q_i + q_j >= D~.
         //
         // Units: NT = 2: every item, this group's column tile (half = group);
+        //        NT = 3: every item, this group's row tile of the pair (half = group);
         //        NT = 1: the items of this group (grp, grp + 2, ...), their only tile.
         const int ew = warp - 2;
         const int grp = ew / kGroupWarps;
         const int sub = warp & 3;                      // TMEM sub-partition this warp may access
         const int cg = (ew % kGroupWarps) >> 2;        // column group: columns [kEpiCols cg, +kEpiCols)
-        const int half = NT == 2 ? grp : 0;
-        const unsigned ustride = NT == 2 ? 1u : (unsigned)kEpiGroups;
-        const uint32_t goff = NT == 2 ? 0u : (uint32_t)grp;  // first unit in a chunk
+        const int half = NH == 2 ? grp : 0;
+        const unsigned ustride = NH == 2 ? 1u : (unsigned)kEpiGroups;
+        const uint32_t goff = NH == 2 ? 0u : (uint32_t)grp;  // first unit in a chunk
         float* colu = (float*)(sm + SL.colinfo) + ew * kColuFloats;
+        // this warp's stage: shared-memory address recomputed where used (a register less)
+        const uint32_t stage_base = smem_u32(sm + SL.stage) + (uint32_t)(ew * kStage * 8);
+        uint32_t fill = 0;  // candidates in this warp's stage (warp-uniform)
+        // writes the stage to the global list after one reservation (the count grows past
+        // the capacity, so that the caller learns the total and regrows the list)
+        auto flush = [&]() {
+            __syncwarp();
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(cand_count, (unsigned long long)fill);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            for (uint32_t k = (uint32_t)lane; k < fill; k += 32)
+                if (base + k < cand_cap) cand[base + k] = st_shared_ld_u2(stage_base + 8 * k);
+            __syncwarp();
+            fill = 0;
+        };
         const int r = sub * 32 + lane;
         // Fragment layout (tcgen05.ld.16x256b): thread (rq, q4) = (lane / 4, lane % 4) holds
         // rows rq + 8 k (k = 0..3) of this sub-partition and columns 8 m + 2 q4 + e
@@ -660,7 +784,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
         float2 tj = make_float2(0.f, 0.f);
         uint32_t w = 0;
         uint32_t local = 0;  // item index in the CTA's sequence
-        ItemPrefetch pf;
+        UnitPrefetch<NT> pf;
         if (drill) {
             // failure drill: wait on a barrier that nothing arrives on; the bounded wait runs
             // out, records the fault and raises the abort flag, and the whole CTA winds down
@@ -671,10 +795,10 @@ __global__ void __maxnreg__(kGramMaxRegs)
         if (have) {
             w = c0 + goff;
             local = base + (uint32_t)goff;
-            pf.init(items, w, cend, ustride);
-            const int4 it = pf.next(w);
+            pf.init(items, w, cend, ustride, half);
+            const int2 it = pf.next(w);
             it_i = it.x;
-            it_j = half ? it.z : it.y;
+            it_j = it.y;
             if (it_j >= 0) {
                 if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
                 ri = rowinfo[(int64_t)it_i * kTile + r];
@@ -706,7 +830,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
             uint32_t ln = local + ustride;
             bool nhave = true;
             {
-                int4 itn;
+                int2 itn;
                 if (wn < cend) {
                     itn = pf.next(wn);
                 } else {
@@ -714,12 +838,12 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     if (nhave) {
                         wn = c0 + goff;
                         ln = base + (uint32_t)goff;
-                        pf.init(items, wn, cend, ustride);
+                        pf.init(items, wn, cend, ustride, half);
                         itn = pf.next(wn);
                     }
                 }
                 it_i = nhave ? itn.x : -1;
-                it_j = nhave ? (half ? itn.z : itn.y) : -1;
+                it_j = nhave ? itn.y : -1;
                 if (nhave && it_j >= 0) {
                     if (!FOLD) uc = reinterpret_cast<const float2*>(ucol)[((int64_t)it_j * kTile + cg * kEpiCols) / 2 + lane];
                     ri = rowinfo[(int64_t)it_i * kTile + r];
@@ -746,7 +870,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 if (lane == 0) mbar_arrive(&tempty[b]);
             } else {
             const uint32_t taddr = tmem_base + ((uint32_t)(sub * 32) << 16) +
-                                   (uint32_t)(b * kAccCols * NT + half * kAccCols + cg * kEpiCols);
+                                   (uint32_t)(b * kAccCols * NH + half * kAccCols + cg * kEpiCols);
             // this thread's column terms: u2[m] = u_j of columns 8 m + 2 q4 + {0, 1}
             float2 u2[8];
 #pragma unroll
@@ -841,16 +965,30 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 }
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
                 if (total > 0) {
-                    unsigned long long base = 0;
-                    if (lane == 31) base = atomicAdd(cand_count, (unsigned long long)total);
-                    base = __shfl_sync(0xffffffffu, base, 31);
-                    unsigned long long pos = base + (unsigned long long)(incl - cnt);
-                    while (msk) {
-                        const int x = __ffs(msk) - 1;
-                        msk &= msk - 1;
-                        if (pos < cand_cap)
-                            cand[pos] = make_uint2((uint32_t)(r0 + 8 * ((x >> 1) & 1)), (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
-                        ++pos;
+                    if (fill + (uint32_t)total > (uint32_t)kStage && fill > 0) flush();
+                    if (total > kStage) {
+                        // more than a stage in one slice: reserved and written directly
+                        unsigned long long base = 0;
+                        if (lane == 31) base = atomicAdd(cand_count, (unsigned long long)total);
+                        base = __shfl_sync(0xffffffffu, base, 31);
+                        unsigned long long pos = base + (unsigned long long)(incl - cnt);
+                        while (msk) {
+                            const int x = __ffs(msk) - 1;
+                            msk &= msk - 1;
+                            if (pos < cand_cap)
+                                cand[pos] = make_uint2((uint32_t)(r0 + 8 * ((x >> 1) & 1)),
+                                                       (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
+                            ++pos;
+                        }
+                    } else {
+                        uint32_t sa = stage_base + 8 * (fill + (uint32_t)(incl - cnt));
+                        while (msk) {
+                            const int x = __ffs(msk) - 1;
+                            msk &= msk - 1;
+                            st_shared_u2(sa, (uint32_t)(r0 + 8 * ((x >> 1) & 1)), (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
+                            sa += 8;
+                        }
+                        fill += (uint32_t)total;
                     }
                 }
             }
@@ -860,6 +998,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
             local = ln;
             have = nhave;
         }
+        if (fill > 0) flush();  // also after an abort: the staged candidates are complete
         (void)alive;
     }
 
@@ -1351,6 +1490,9 @@ static void gram_dispatch_fold(int kch, int nt, Args... args)
     if (nt == 2) {
         if (kch == 1) gram_instance<1, 2, FOLD, false>(args...);
         else gram_instance<2, 2, FOLD, false>(args...);
+    } else if (nt == 3) {
+        if (kch == 1) gram_instance<1, 3, FOLD, false>(args...);
+        else gram_instance<2, 3, FOLD, false>(args...);
     } else {
         switch (kch) {
             case 1: gram_instance<1, 1, FOLD, false>(args...); break;
@@ -1393,6 +1535,7 @@ GramTune gram_tune(rnng_ctx* c, int kind, int dp, int64_t tile_pairs)
     t.dp = dp;
     // two column tiles per item (N = 256 MMAs) while two B slots of them fit next to A
     t.nt = (kind == 0 && dp <= 2 * kChunkK) ? 2 : 1;
+    const int nt_table = t.nt;
     t.chunk = 64;
     t.slots = 0;
     const GramTune* best = nullptr;
@@ -1406,8 +1549,10 @@ GramTune gram_tune(rnng_ctx* c, int kind, int dp, int64_t tile_pairs)
         if (r->chunk > 0) t.chunk = r->chunk;
         if (r->slots > 0) t.slots = r->slots;
     }
-    // compiled forms: two column tiles only for BF16 operands of at most two K-chunks
-    if (kind != 0 || dp > 2 * kChunkK || t.nt != 2) t.nt = 1;
+    // compiled forms: two column tiles (nt = 2) and row pairs (nt = 3) only for BF16
+    // operands of at most two K-chunks
+    if (t.nt < 1 || t.nt > 3) t.nt = nt_table;
+    if (kind != 0 || dp > 2 * kChunkK) t.nt = 1;
     t.chunk = std::max(1, std::min(t.chunk, 1 << 20));
     // with one column tile the two epilogue groups take alternate items of a chunk: even sizes
     if (t.nt == 1) t.chunk = (t.chunk + 1) & ~1;
@@ -1619,7 +1764,9 @@ extern "C" int rnng_gram_probe_bf16(rnng_ctx* c, const float* X, int64_t d, floa
         RNNG_CUDA(cudaMemcpyAsync(c->items.ptr, &item, sizeof(int4), cudaMemcpyHostToDevice, s));
         L.items = c->items.as<int4>();
         L.num_items = 1;
-        L.item_tiles = gram_tune(c, 0, (int)d, 1).nt;
+        // the probe's one item is a row tile with one column tile (the row-pair form only
+        // changes which resident A tile the MMAs read)
+        L.item_tiles = std::min(2, gram_tune(c, 0, (int)d, 1).nt);
         L.gram_chunk = 2;
         c->aux7.reserve(sizeof(float) * (size_t)n * n);
         L.gram_raw = c->aux7.as<float>();

@@ -1,8 +1,9 @@
 """Autotuner of the tensor-core Gram kernel.
 
-Sweeps the kernel's three knobs on the benchmark configurations - column tiles per item
-(nt: one 128-column tile, or two for N = 256 MMAs), items per work-queue chunk, and B
-operand slots per CTA - and writes the fastest setting per (operand kind, padded width,
+Sweeps the kernel's three knobs on the benchmark configurations - the item form (nt: one
+row tile with one 128-column tile, or with two for N = 256 MMAs, or 3: two row tiles
+sharing one column tile), items per work-queue chunk, and B operand slots per CTA - and
+writes the fastest setting per (operand kind, padded width,
 tile-pair count) to rnng_gb300/gram_tuning.json.  The library reads that table when a
 context is created (rnng_ctx_set_gram_tuning overrides it per context).
 
@@ -83,7 +84,7 @@ def main():
 
         base_ms, edges, st = timed(0, 0, 0)
         pairs = int(st["tile_pairs"])
-        nts = (1, 2) if kind == "bf16" and dp <= 128 else (1,)
+        nts = (1, 2, 3) if kind == "bf16" and dp <= 128 else (1,)
         results = []
         t0 = time.time()
         for nt in nts:

@@ -48,6 +48,28 @@ def test_random_against_oracle(ctx, orc, mode, case):
     assert same(got, want), (len(got[0]), len(want[0]))
 
 
+@pytest.mark.parametrize("nt", [1, 2, 3])
+@pytest.mark.parametrize("case", CASES)
+def test_item_forms_against_oracle(ctx, orc, case, nt):
+    """Every item form of the Gram kernel - one row tile with one or two column tiles, or a
+    pair of row tiles with one column tile (odd and even tile counts) - gives RNNG's edges,
+    with small queue chunks so that even these sizes take many chunks."""
+    n, d, scale, r, seed = case
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10, 10, size=(8, d))
+    x = (centres[rng.integers(0, 8, n)] + scale * rng.normal(size=(n, d))).astype(np.float32)
+    want = orc.eps_graph_l2(x, np.float32(r))
+    ctx.set_gram_tuning(nt, 5, 0)
+    try:
+        got = ctx.eps_graph_l2(x, np.float32(r), mode="bf16")
+        st = ctx.stats()
+    finally:
+        ctx.set_gram_tuning(0, 0, 0)
+    assert same(got, want), (len(got[0]), len(want[0]))
+    if st["gram_nt"] and d <= 128:
+        assert st["gram_nt"] == nt
+
+
 @pytest.mark.parametrize("mode", MODES)
 def test_edge_cases(ctx, orc, mode):
     # empty and single point
@@ -240,7 +262,7 @@ def test_gram_tuning_table_and_override(ctx, orc):
     assert st["tile_pairs"] < max(t["min_pairs"] for t in table if t["dp"] == 64) or len(table) == 1
     assert (st["gram_nt"], st["gram_chunk"]) == (row["nt"], row["chunk"])
     assert same(got, want)
-    for nt, chunk, slots in ((2, 1, 2), (1, 2, 3), (2, 7, 0), (1, 5, 2)):
+    for nt, chunk, slots in ((2, 1, 2), (1, 2, 3), (2, 7, 0), (1, 5, 2), (3, 1, 2), (3, 9, 0)):
         ctx.set_gram_tuning(nt, chunk, slots)
         got = ctx.eps_graph_l2(x, r, mode="bf16")
         st = ctx.stats()

@@ -72,6 +72,11 @@ def lib() -> ctypes.CDLL:
                                       ctypes.c_float, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_i64p),
                                       ctypes.POINTER(_i64p), ctypes.POINTER(_f32p),
                                       ctypes.POINTER(ctypes.c_double), _i64p]
+        L.orc_landmark_edit.restype = ctypes.c_int64
+        L.orc_landmark_edit.argtypes = [ctypes.c_void_p, _i64p, ctypes.c_int64, ctypes.c_float, ctypes.c_int64,
+                                        ctypes.c_float, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_i64p),
+                                        ctypes.POINTER(_i64p), ctypes.POINTER(_f32p),
+                                        ctypes.POINTER(ctypes.c_double), _i64p]
         L.orc_free.argtypes = [ctypes.c_void_p]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -142,6 +147,25 @@ def landmark_l2(X: np.ndarray, eps, num_centers: int, cover: float = 1.5, leaf_s
     cnt = lib().orc_landmark_l2(X.ctypes.data_as(_f32p), n, d, ctypes.c_float(eps), num_centers,
                                 ctypes.c_float(cover), leaf_size, seed, ctypes.byref(pu), ctypes.byref(pv),
                                 ctypes.byref(pw), ph, st)
+    info = {k: ph[i] for i, k in enumerate(LANDMARK_PHASES)}
+    info.update({"seconds": sum(ph), "num_cells": int(st[0]), "num_ghosts": int(st[1]), "threads": int(st[2]),
+                 "empty_cells": int(st[3])})
+    return _edges(cnt, pu, pv, pw, sort=False), info
+
+
+def landmark_edit(atoms: np.ndarray, offsets: np.ndarray, eps, num_centers: int, cover: float = 1.5,
+                  leaf_size: int = 10, seed: int = 7):
+    """The same pipeline over strings under RNNG's edit distance (its driver's `-D edit`
+    path): (u, v, w) and the phase dict, as landmark_l2."""
+    atoms = np.ascontiguousarray(atoms, np.uint8)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    n = offsets.size - 1
+    pu, pv, pw = _i64p(), _i64p(), _f32p()
+    ph = (ctypes.c_double * 5)()
+    st = (ctypes.c_int64 * 4)()
+    cnt = lib().orc_landmark_edit(atoms.ctypes.data_as(ctypes.c_void_p), offsets.ctypes.data_as(_i64p), n,
+                                  ctypes.c_float(eps), num_centers, ctypes.c_float(cover), leaf_size, seed,
+                                  ctypes.byref(pu), ctypes.byref(pv), ctypes.byref(pw), ph, st)
     info = {k: ph[i] for i, k in enumerate(LANDMARK_PHASES)}
     info.update({"seconds": sum(ph), "num_cells": int(st[0]), "num_ghosts": int(st[1]), "threads": int(st[2]),
                  "empty_cells": int(st[3])})

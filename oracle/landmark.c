@@ -29,7 +29,9 @@
  *                  cell's own points and of its ghosts)
  *   graph          include/graph.hpp:59-116 (edges sorted and deduplicated; kept here as
  *                  unordered pairs u < v)
- * Distances are orc_l2seq (drivers/systolic.cpp:253-269).  Cells run in parallel on the
+ * Distances are orc_l2seq (drivers/systolic.cpp:253-269) for float rows, or orc_edit
+ * (drivers/systolic.cpp:271-299) for strings (orc_landmark_edit: the driver's `-D edit`
+ * path; the trees, ghosts and queries only see the metric).  Cells run in parallel on the
  * host threads, largest first (RNNG's ranks take cells by the same longest-first rule,
  * include/point.hpp:596-605); the Voronoi and ghost queries run in parallel over points.
  */
@@ -45,6 +47,7 @@
 #endif
 
 float orc_l2seq(const float* p, const float* q, int64_t d);
+float orc_edit(const uint8_t* s, int64_t m, const uint8_t* t, int64_t n);
 
 /* ---------------------------------------------------------------- growable arrays */
 
@@ -85,15 +88,35 @@ static double now_s(void)
 
 /* ---------------------------------------------------------------- point sets */
 
-/* A point set: rows of X named by global row indices (a cell, its ghosts, the centres). */
+/* The points and their metric: rows of X (n x d) under orc_l2seq, or, when atoms is set,
+ * the strings atoms[offs[i] .. offs[i+1]) under orc_edit (RNNG's two Distance functors,
+ * drivers/landmark.cpp:335-383). */
 typedef struct {
     const float* X;
     int64_t d;
+    const uint8_t* atoms;
+    const int64_t* offs;
+} metric;
+
+static inline float mdist(const metric* M, int64_t a, int64_t b)
+{
+    if (M->atoms)
+        return orc_edit(M->atoms + M->offs[a], M->offs[a + 1] - M->offs[a], M->atoms + M->offs[b],
+                        M->offs[b + 1] - M->offs[b]);
+    return orc_l2seq(M->X + a * M->d, M->X + b * M->d, M->d);
+}
+
+/* A point set: points named by global row indices (a cell, its ghosts, the centres). */
+typedef struct {
+    const metric* M;
     const int64_t* rows;
     int64_t n;
 } pset;
 
-static inline const float* P(const pset* s, int64_t i) { return s->X + s->rows[i] * s->d; }
+/* distance between local point i of s and local point j of t */
+static inline float D(const pset* s, int64_t i, const pset* t, int64_t j) { return mdist(s->M, s->rows[i], t->rows[j]); }
+/* distance between local point i of s and global row q */
+static inline float Dq(const pset* s, int64_t i, int64_t q) { return mdist(s->M, s->rows[i], q); }
 
 /* ---------------------------------------------------------------- cover tree */
 
@@ -180,7 +203,7 @@ static void ctree_build(ctree* t, const pset* s, float cover, int64_t leaf_size)
     root.radius = 0.0f;
     root.candidate = 0;
     for (int64_t i = 0; i < n; ++i) {
-        const float di = orc_l2seq(P(s, 0), P(s, i), s->d);
+        const float di = D(s, 0, s, i);
         iv_push(&root.ids, i);
         iv_push(&root.cells, 0);
         fv_push(&root.dists, di);
@@ -205,7 +228,7 @@ static void ctree_build(ctree* t, const pset* s, float cover, int64_t leaf_size)
             h.candidate = 0;
             sep = 0.0f;
             for (int64_t j = 0; j < m; ++j) {
-                const float dj = orc_l2seq(P(s, nc), P(s, h.ids.p[j]), s->d);
+                const float dj = D(s, nc, s, h.ids.p[j]);
                 if (dj < h.dists.p[j]) {
                     h.dists.p[j] = dj;
                     h.cells.p[j] = nc;
@@ -312,8 +335,9 @@ static int64_t iq_pop(iq* q)
     return q->p[q->head++];
 }
 
-/* CoverTree::radius_query: every point within r of the query, appended to out (local ids). */
-static void ctree_query(const ctree* t, const pset* s, const float* query, float r, ivec* out, iq* q)
+/* CoverTree::radius_query: every point within r of the query (a global row), appended to
+ * out (local ids). */
+static void ctree_query(const ctree* t, const pset* s, int64_t query, float r, ivec* out, iq* q)
 {
     if (s->n == 0) return;
     q->head = q->n = 0;
@@ -321,18 +345,18 @@ static void ctree_query(const ctree* t, const pset* s, const float* query, float
     while (q->n > 0) {
         const int64_t u = iq_pop(q);
         if (t->cptr[u] == t->cptr[u + 1]) {
-            if (orc_l2seq(P(s, t->center[u]), query, s->d) <= r) iv_push(out, t->center[u]);
+            if (Dq(s, t->center[u], query) <= r) iv_push(out, t->center[u]);
             continue;
         }
         for (int64_t k = t->cptr[u]; k < t->cptr[u + 1]; ++k) {
             const int64_t c = t->child[k];
-            if (orc_l2seq(P(s, t->center[c]), query, s->d) <= t->radius[c] + r) iq_push(q, c);
+            if (Dq(s, t->center[c], query) <= t->radius[c] + r) iq_push(q, c);
         }
     }
 }
 
 /* CoverTree::has_radius_neighbor: breadth first, stops at the first point within r. */
-static int ctree_has_neighbor(const ctree* t, const pset* s, const float* query, float r, iq* q)
+static int ctree_has_neighbor(const ctree* t, const pset* s, int64_t query, float r, iq* q)
 {
     if (s->n == 0) return 0;
     q->head = q->n = 0;
@@ -340,12 +364,12 @@ static int ctree_has_neighbor(const ctree* t, const pset* s, const float* query,
     while (q->n > 0) {
         const int64_t u = iq_pop(q);
         if (t->cptr[u] == t->cptr[u + 1]) {
-            if (orc_l2seq(P(s, t->center[u]), query, s->d) <= r) return 1;
+            if (Dq(s, t->center[u], query) <= r) return 1;
             continue;
         }
         for (int64_t k = t->cptr[u]; k < t->cptr[u + 1]; ++k) {
             const int64_t c = t->child[k];
-            if (orc_l2seq(P(s, t->center[c]), query, s->d) <= t->radius[c] + r) iq_push(q, c);
+            if (Dq(s, t->center[c], query) <= t->radius[c] + r) iq_push(q, c);
         }
     }
     return 0;
@@ -383,11 +407,10 @@ static void ctree_query_batched(const ctree* t, const pset* s, const pset* batch
         item it = stack[--sn];
         if (t->cptr[it.u] == t->cptr[it.u + 1]) {
             const int64_t leaf = t->center[it.u];
-            const float* pl = P(s, leaf);
             const int64_t pid = s->rows[leaf];
             for (int64_t k = 0; k < it.n; ++k) {
                 const int64_t qi = it.ids[k];
-                const float dist = orc_l2seq(pl, P(batch, qi), s->d);
+                const float dist = D(s, leaf, batch, qi);
                 const int64_t qid = batch->rows[qi];
                 if (dist <= r && qid != pid) {
                     iv_push(&out->u, qid < pid ? qid : pid);
@@ -399,11 +422,11 @@ static void ctree_query_batched(const ctree* t, const pset* s, const pset* batch
             for (int64_t k = t->cptr[it.u]; k < t->cptr[it.u + 1]; ++k) {
                 const int64_t c = t->child[k];
                 const float eps = t->radius[c] + r;
-                const float* pc = P(s, t->center[c]);
+                const int64_t pc = t->center[c];
                 int64_t* keep = (int64_t*)malloc((size_t)it.n * sizeof(int64_t));
                 int64_t nk = 0;
                 for (int64_t j = 0; j < it.n; ++j)
-                    if (orc_l2seq(pc, P(batch, it.ids[j]), s->d) <= eps) keep[nk++] = it.ids[j];
+                    if (D(s, pc, batch, it.ids[j]) <= eps) keep[nk++] = it.ids[j];
                 if (nk == 0) {
                     free(keep);
                     continue;
@@ -472,9 +495,9 @@ static int cmp_edge(const void* a, const void* b)
  * can land in the wrong cells and edges between cells go missing; this port keeps that
  * behaviour.
  */
-int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int64_t num_centers, float cover,
-                        int64_t leaf_size, uint64_t seed, int64_t** ou, int64_t** ov, float** ow, double* phase_s,
-                        int64_t* stats)
+static int64_t landmark_core(const metric* M, int64_t n, float radius, int64_t num_centers, float cover,
+                             int64_t leaf_size, uint64_t seed, int64_t** ou, int64_t** ov, float** ow, double* phase_s,
+                             int64_t* stats)
 {
     double t0 = now_s();
     const int nt0 =
@@ -516,7 +539,7 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
         float best = FLT_MAX;
         int64_t bc = 0;
         for (int64_t c = 0; c < num_centers; ++c) {
-            const float dc = orc_l2seq(X + lm[c] * d, X + i * d, d);
+            const float dc = mdist(M, lm[c], i);
             if (dc <= best) {
                 best = dc;
                 bc = c;
@@ -558,7 +581,7 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
     int64_t* order = (int64_t*)malloc((size_t)num_centers * sizeof(int64_t));
     for (int64_t c = 0; c < num_centers; ++c) {
         order[c] = c;
-        sets[c] = (pset){X, d, cells[c].rows, cells[c].n};
+        sets[c] = (pset){M, cells[c].rows, cells[c].n};
     }
     sort_cells(order, num_centers, cells);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -567,7 +590,7 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
     int64_t nne = 0;
     for (int64_t c = 0; c < num_centers; ++c)
         if (cells[c].n > 0) slot0[nne++] = cells[c].rows[0];
-    pset centres = {X, d, slot0, nne};
+    pset centres = {M, slot0, nne};
     ctree ctr;
     ctree_build(&ctr, &centres, cover, 1);
     /* every point in cell order, with its own cell (the cell index of RNNG's sendbuf) */
@@ -594,7 +617,7 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
         iq q = {0};
 #pragma omp for schedule(dynamic, 256)
         for (int64_t k = 0; k < n; ++k) {
-            const float* xq = X + qrow[k] * d;
+            const int64_t xq = qrow[k];
             found.n = 0;
             ctree_query(&ctr, &centres, xq, qdist[k] + two_r, &found, &q);
             for (int64_t j = 0; j < found.n; ++j) {
@@ -630,7 +653,7 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
 #else
             0;
 #endif
-        pset gh = {X, d, cells[c].ghosts.p, cells[c].ghosts.n};
+        pset gh = {M, cells[c].ghosts.p, cells[c].ghosts.n};
         ctree_query_batched(&trees[c], &sets[c], &sets[c], radius, &eb[tid]);
         ctree_query_batched(&trees[c], &sets[c], &gh, radius, &eb[tid]);
     }
@@ -699,4 +722,22 @@ int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int6
     free(dist_of);
     free(perm);
     return mu;
+}
+
+int64_t orc_landmark_l2(const float* X, int64_t n, int64_t d, float radius, int64_t num_centers, float cover,
+                        int64_t leaf_size, uint64_t seed, int64_t** ou, int64_t** ov, float** ow, double* phase_s,
+                        int64_t* stats)
+{
+    const metric M = {X, d, NULL, NULL};
+    return landmark_core(&M, n, radius, num_centers, cover, leaf_size, seed, ou, ov, ow, phase_s, stats);
+}
+
+/* The same pipeline over strings under RNNG's edit distance (the driver's `-D edit` path,
+ * drivers/landmark.cpp:61-62). */
+int64_t orc_landmark_edit(const uint8_t* atoms, const int64_t* offsets, int64_t n, float radius, int64_t num_centers,
+                          float cover, int64_t leaf_size, uint64_t seed, int64_t** ou, int64_t** ov, float** ow,
+                          double* phase_s, int64_t* stats)
+{
+    const metric M = {NULL, 0, atoms, offsets};
+    return landmark_core(&M, n, radius, num_centers, cover, leaf_size, seed, ou, ov, ow, phase_s, stats);
 }

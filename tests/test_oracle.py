@@ -203,6 +203,23 @@ def test_landmark_pipeline_port_matches_brute_force(orc, name, centres):
     orc.set_threads(full)
 
 
+@pytest.mark.parametrize("centres", [1, 7, 40])
+def test_landmark_pipeline_port_edit_distance(orc, centres):
+    """The same pipeline under RNNG's edit distance (its driver's `-D edit` path) finds
+    the edges RNNG's own driver found on the DNA fixture, on one thread and on all."""
+    g = golden("k3_edit")
+    full = orc.num_threads()
+    for threads in (1, full):
+        orc.set_threads(threads)
+        (u, v, w), info = orc.landmark_edit(g["atoms"], g["offsets"], g["radius"], num_centers=centres)
+        order = np.lexsort((v, u))
+        u, v, w = u[order], v[order], w[order]
+        assert np.array_equal(u, g["u"]) and np.array_equal(v, g["v"])
+        assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+        assert info["num_cells"] == centres and info["threads"] == threads
+    orc.set_threads(full)
+
+
 def test_landmark_pipeline_port_duplicates_and_tiny(orc):
     rng = np.random.default_rng(5)
     x = np.repeat(rng.normal(size=(40, 5)).astype(np.float32), 7, axis=0)

@@ -140,6 +140,50 @@ def cpu_landmark_leg(x, radius, prefix: int = LANDMARK_PREFIX, centres: int | No
             "phases_s": {k: round(info[k], 3) for k in oracle.LANDMARK_PHASES}}
 
 
+K3_PREFIX = 8_000   # strings of the edit-distance CPU sample: 200 whole families of 40
+K3_FAMILY = 40      # strings per family; RNNG's run of the workload: 5,000 landmarks for 200k strings
+
+
+def cpu_edit_leg(seqs, radius, prefix: int = K3_PREFIX) -> dict:
+    """RNNG's landmark pipeline under edit distance (its driver's `-D edit` path, restated in
+    oracle/landmark.c) over the first `prefix` strings, with one landmark per family's worth
+    of strings.  The strings come family by family, so the prefix keeps each string's
+    relatives; RNNG's cost per edge grows with n (Voronoi is n x landmarks edit distances),
+    so the sample's rate is an upper bound of its full-size rate."""
+    import oracle
+    from rnng_gb300 import synth
+    oracle.build()
+    atoms, offsets = synth.pack_seqs(seqs[:prefix])
+    m = max(1, prefix // K3_FAMILY)
+    t0 = time.perf_counter()
+    (u, v, w), info = oracle.landmark_edit(atoms, offsets, radius, num_centers=m)
+    dt = time.perf_counter() - t0
+    return {"value": u.size / dt, "edges": int(u.size), "seconds": dt, "points": prefix, "landmarks": m,
+            "threads": info["threads"], "host_cores": os.cpu_count(),
+            "phases_s": {k: round(info[k], 3) for k in oracle.LANDMARK_PHASES}}
+
+
+def cpu_rips_leg(x, radius, landmarks_per_500k: int = 1024) -> dict:
+    """The Rips workload on the host: RNNG's landmark epsilon graph (oracle/landmark.c, its
+    driver's 1,024 landmarks) over all points, then the filtration - every clique up to a
+    triangle with its value, sorted by (value, id) as RNNG's merge does (oracle orc_rips,
+    one thread).  Simplices/s of the whole job."""
+    import oracle
+    oracle.build()
+    n = x.shape[0]
+    m = max(1, n * landmarks_per_500k // 500_000)
+    t0 = time.perf_counter()
+    (u, v, w), info = oracle.landmark_l2(x, radius, num_centers=m)
+    t1 = time.perf_counter()
+    ids, _ = oracle.rips(n, u, v, w, 2)
+    t2 = time.perf_counter()
+    phases = {k: round(info[k], 3) for k in oracle.LANDMARK_PHASES}
+    phases["filtration"] = round(t2 - t1, 3)
+    return {"value": ids.size / (t2 - t0), "simplices": int(ids.size), "edges": int(u.size), "graph_s": t1 - t0,
+            "rips_s": t2 - t1, "points": n, "landmarks": m, "threads": info["threads"],
+            "host_cores": os.cpu_count(), "phases_s": phases}
+
+
 def landmark_sample_text(leg: dict) -> str:
     return (f"RNNG's landmark pipeline (oracle/landmark.c) on the first {leg['points']} points, "
             f"{leg['landmarks']} landmarks, {leg['threads']} host threads of {leg['host_cores']} cores: "
@@ -508,6 +552,27 @@ def run_secondary(args, world, rank, local):
                "algorithm": "RNNG cover-tree search" + (" (one cell: systolic)" if wl == "k1" else
                                                         " with landmark cells and ghosts"),
                "sample": landmark_sample_text(leg), "phases_s": leg["phases_s"]}
+    if rank == 0 and not args.no_cpu and wl == "k3":
+        leg = cpu_edit_leg(seqs, radius)
+        cpu = {"value": leg["value"], "unit": SECONDARY[wl]["unit"], "cores": leg["threads"], "kind": "port",
+               "algorithm": "RNNG cover-tree search under edit distance with landmark cells and ghosts",
+               "sample": (f"RNNG's landmark pipeline under edit distance (oracle/landmark.c) on the first "
+                          f"{leg['points']} strings ({leg['points'] // K3_FAMILY} whole families), {leg['landmarks']} "
+                          f"landmarks (one per {K3_FAMILY} strings, as RNNG's run of this workload), "
+                          f"{leg['threads']} host threads of {leg['host_cores']} cores: {leg['edges']} edges in "
+                          f"{leg['seconds']:.2f} s"),
+               "phases_s": leg["phases_s"]}
+    if rank == 0 and not args.no_cpu and wl == "k4":
+        leg = cpu_rips_leg(x, radius)
+        cpu = {"value": leg["value"], "unit": SECONDARY[wl]["unit"], "cores": leg["threads"], "kind": "port",
+               "algorithm": "RNNG landmark epsilon graph, then clique enumeration and (value, id) order",
+               "sample": (f"the whole workload ({leg['points']} points): RNNG's landmark pipeline (oracle/landmark.c, "
+                          f"{leg['landmarks']} landmarks, {leg['threads']} host threads of {leg['host_cores']} cores) "
+                          f"{leg['edges']} edges in {leg['graph_s']:.2f} s, then the filtration of cliques up to "
+                          f"triangles sorted by (value, id) (oracle orc_rips, one thread) in {leg['rips_s']:.2f} s: "
+                          f"{leg['simplices']} simplices"),
+               "phases_s": leg["phases_s"]}
+        assert leg["simplices"] == units, (leg["simplices"], units)
     roofline = None
     if wl == "k3" and last["ms_gram"] > 0:
         # the filter: a Gram form over 512-byte E4M3 rows (thermometer-coded q-gram profiles)
@@ -528,12 +593,16 @@ def run_secondary(args, world, rank, local):
         # a K5 step is a third of a second of Gram work: the sustained peak applies
         peak, src = (sustained, src + " (sustained bf16)") if wl == "k5" else (burst, src + " (burst bf16)")
         dp = -(-d // 64) * 64
-        flops = 2.0 * dp * last["pairs_evaluated"]
-        achieved = flops / (statistics.median(s["ms_gram"] for s in stats) / 1e3) / 1e12
+        ms_gram = statistics.median(s["ms_gram"] for s in stats)
+        achieved = 2.0 * d * last["pairs_evaluated"] / (ms_gram / 1e3) / 1e12
+        # the tensor cores multiply the padded width: dp - d columns are zeros or the folded column terms
+        issued = 2.0 * dp * last["pairs_evaluated"] / (ms_gram / 1e3) / 1e12
         roofline = {"bound": "tensor", "kernel": "k_gram_bf16", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak, "peak_source": src, "frac_burst": achieved / burst,
                     "frac_sustained": achieved / sustained, "traffic": None,
-                    "algorithmic": "2*dp flops per evaluated pair (dp = d padded to 64)"}
+                    "algorithmic": "2*d flops per evaluated pair",
+                    "mma_issued": {"achieved": issued, "frac": issued / peak,
+                                   "counted": f"2*dp flops per evaluated pair (dp = {dp}, d padded to 64)"}}
     if rank == 0:
         cfg.update({"units": int(units), "parallelism": "replicas" if world > 1 else "single-gpu",
                     "stage_ms": {k: round(last[k], 3) for k in ("ms_partition", "ms_bounds", "ms_prune", "ms_tiles",

@@ -253,6 +253,25 @@ __device__ __forceinline__ void tmem_ld16x256b_x8(uint32_t taddr, float* v)
 
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// tcgen05.ld.red.32x32b.x32 (sm_103a) and its wait, in one statement so that no use of the
+// registers can be scheduled before the load lands: thread t gets TMEM lane (lane field
+// of taddr) + t, the 32 columns from taddr's column on, and their maximum.
+__device__ __forceinline__ float tmem_ld_max_32x32b_x32(uint32_t taddr, float* v)
+{
+    float m;
+    asm volatile(
+        "tcgen05.ld.red.sync.aligned.32x32b.x32.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, %32, [%33];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
+          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]),
+          "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]),
+          "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31]), "=f"(m)
+        : "r"(taddr)
+        : "memory");
+    return m;
+}
+
 // 8-byte shared-memory store and load at a shared-window address.
 __device__ __forceinline__ void st_shared_u2(uint32_t addr, uint32_t a, uint32_t b)
 {
@@ -817,12 +836,14 @@ __global__ void __maxnreg__(kGramMaxRegs)
             // thread (., q) reads its 16 terms as four 16-byte loads, the four q rows in distinct banks
             if (!FOLD) reinterpret_cast<float2*>(colu)[(lane & 3) * 10 + (lane >> 2)] = uc;
             float Wk[4];
+            float Wi;  // the threshold of row r (this lane's row of the sub-partition)
             {
                 const float A = eps_p + ri.y;
                 const float AA = A * A, cross = 2.f * A * tj.x;
-                const float Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
+                Wi = (AA + ri.z - ri.x + cross) + kappa * (ri.x + tj.y + AA + ri.z + cross);
+                if (!FOLD)
 #pragma unroll
-                for (int k = 0; k < 4; ++k) Wk[k] = __shfl_sync(0xffffffffu, Wi, rq + 8 * k);
+                    for (int k = 0; k < 4; ++k) Wk[k] = __shfl_sync(0xffffffffu, Wi, rq + 8 * k);
             }
             // the next unit (in this chunk, or the first of the next one) and its loads, issued
             // now: they complete while this unit is tested
@@ -880,6 +901,42 @@ __global__ void __maxnreg__(kGramMaxRegs)
                 u2[2 * t + 1] = make_float2(v.z, v.w);
             }
             for (int hh = 0; hh < 2; ++hh) {
+                uint32_t msk = 0;
+                // candidate x of this thread is (r0, c0 + x) in the FOLD layout, else
+                // (r0 + 8 ((x >> 1) & 1), c0 + 8 (x >> 2) + (x & 1))
+                int r0, c0;
+                if constexpr (FOLD) {
+                    // 32x32b layout: this thread's row is lane r of the sub-partition, the load
+                    // brings columns 32 hh .. 32 hh + 31 of the warp's 64 and their maximum
+                    // (tcgen05.ld.red).  The accumulator holds g - u_j / 2, so the term
+                    // -2 g + u_j is -2 g (exact) and the row's smallest term is -2 max g.
+                    float g[32];
+                    const float gmax = tmem_ld_max_32x32b_x32(taddr + 32u * (uint32_t)hh, g);
+                    if (hh == 1) {
+                        // accumulator slice read: hand it back to the MMA warp
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&tempty[b]);
+                    }
+                    const bool mine = -2.f * gmax <= Wi;
+                    if (!__any_sync(0xffffffffu, mine)) continue;
+                    r0 = rb - rq + lane;
+                    c0 = cb - 2 * q4 + 32 * hh;
+                    if (mine) {
+                        if (!diag && r0 < n32 && c0 + 31 < n32) {
+#pragma unroll
+                            for (int x = 0; x < 32; ++x) msk |= (-2.f * g[x] <= Wi ? 1u : 0u) << x;
+                        } else {
+#pragma unroll
+                            for (int x = 0; x < 32; ++x) {
+                                const int gj = c0 + x;
+                                // padding rows / columns and, inside a diagonal tile, j <= i excluded
+                                const bool ok = -2.f * g[x] <= Wi && r0 < n32 && gj < n32 && (!diag || gj > r0);
+                                msk |= (ok ? 1u : 0u) << x;
+                            }
+                        }
+                    }
+                } else {
                 // lanes 16 hh .. 16 hh + 15 of the sub-partition, all 64 columns:
                 // g[4 m + 2 hi + e] = row rq + 8 hi + 16 hh, column 8 m + 2 q4 + e
                 float g[32];
@@ -897,65 +954,51 @@ __global__ void __maxnreg__(kGramMaxRegs)
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[b]);
                 }
-                // most rows have no candidate: test each row's minimum term first
+                // most rows have no candidate: test each row's minimum term first.  Packed
+                // pairs: __ffma2_rn forms two terms -2 g + u_j, each rounded once as fmaf; a
+                // three-input minimum takes both into one of the row's running minima
                 float mk[4];
-                if constexpr (FOLD) {
-                    // g holds g - u_j / 2, so the term -2 g + u_j is -2 g (exact): keep each row's
-                    // maximum of g (three-input maxima) and scale it once
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) mk[q] = -INFINITY;
+                for (int q = 0; q < 4; ++q) mk[q] = INFINITY;
+                const float2 k2 = make_float2(-2.f, -2.f);
 #pragma unroll
-                    for (int m = 0; m < 8; ++m)
+                for (int m = 0; m < 8; ++m)
 #pragma unroll
-                        for (int hi = 0; hi < 2; ++hi) {
-                            const int x = 4 * m + 2 * hi;
-                            mk[2 * hi + (m & 1)] = max3f(mk[2 * hi + (m & 1)], g[x], g[x + 1]);
-                        }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) mk[q] *= -2.f;
-                } else {
-                    // packed pairs: __ffma2_rn forms two terms -2 g + u_j, each rounded once as
-                    // fmaf; a three-input minimum takes both into one of the row's running minima
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) mk[q] = INFINITY;
-                    const float2 k2 = make_float2(-2.f, -2.f);
-#pragma unroll
-                    for (int m = 0; m < 8; ++m)
-#pragma unroll
-                        for (int hi = 0; hi < 2; ++hi) {
-                            const int x = 4 * m + 2 * hi;
-                            const float2 p = __ffma2_rn(make_float2(g[x], g[x + 1]), k2, u2[m]);
-                            g[x] = p.x;  // g now holds the terms
-                            g[x + 1] = p.y;
-                            mk[2 * hi + (m & 1)] = min3f(mk[2 * hi + (m & 1)], p.x, p.y);
-                        }
-                }
+                    for (int hi = 0; hi < 2; ++hi) {
+                        const int x = 4 * m + 2 * hi;
+                        const float2 p = __ffma2_rn(make_float2(g[x], g[x + 1]), k2, u2[m]);
+                        g[x] = p.x;  // g now holds the terms
+                        g[x + 1] = p.y;
+                        mk[2 * hi + (m & 1)] = min3f(mk[2 * hi + (m & 1)], p.x, p.y);
+                    }
                 const float W0 = Wk[2 * hh], W1 = Wk[2 * hh + 1];
                 const bool mine = fminf(mk[0], mk[1]) <= W0 || fminf(mk[2], mk[3]) <= W1;
                 if (!__any_sync(0xffffffffu, mine)) continue;
-                const int r0 = rb + 16 * hh;
-                uint32_t msk = 0;
+                r0 = rb + 16 * hh;
+                c0 = cb;
                 if (mine) {
                     // all 2 rows x 16 columns real and off the diagonal tile: the test alone
                     if (!diag && r0 + 8 < n32 && cb + 57 < n32) {
 #pragma unroll
-                        for (int x = 0; x < 32; ++x) {
-                            const float term = FOLD ? -2.f * g[x] : g[x];
-                            msk |= (term <= ((x & 2) ? W1 : W0) ? 1u : 0u) << x;
-                        }
+                        for (int x = 0; x < 32; ++x) msk |= (g[x] <= ((x & 2) ? W1 : W0) ? 1u : 0u) << x;
                     } else {
 #pragma unroll
                         for (int x = 0; x < 32; ++x) {
                             const int gi = r0 + 8 * ((x >> 1) & 1);
                             const int gj = cb + 8 * (x >> 2) + (x & 1);
                             // padding rows / columns and, inside a diagonal tile, j <= i excluded
-                            const float term = FOLD ? -2.f * g[x] : g[x];
-                            const bool ok =
-                                term <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
+                            const bool ok = g[x] <= ((x & 2) ? W1 : W0) && gi < n32 && gj < n32 && (!diag || gj > gi);
                             msk |= (ok ? 1u : 0u) << x;
                         }
                     }
                 }
+                }
+                const auto cand_i = [&](int x) -> uint32_t {
+                    return FOLD ? (uint32_t)r0 : (uint32_t)(r0 + 8 * ((x >> 1) & 1));
+                };
+                const auto cand_j = [&](int x) -> uint32_t {
+                    return FOLD ? (uint32_t)(c0 + x) : (uint32_t)(c0 + 8 * (x >> 2) + (x & 1));
+                };
                 const int cnt = __popc(msk);
                 int incl = cnt;
 #pragma unroll
@@ -975,9 +1018,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                         while (msk) {
                             const int x = __ffs(msk) - 1;
                             msk &= msk - 1;
-                            if (pos < cand_cap)
-                                cand[pos] = make_uint2((uint32_t)(r0 + 8 * ((x >> 1) & 1)),
-                                                       (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
+                            if (pos < cand_cap) cand[pos] = make_uint2(cand_i(x), cand_j(x));
                             ++pos;
                         }
                     } else {
@@ -985,7 +1026,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
                         while (msk) {
                             const int x = __ffs(msk) - 1;
                             msk &= msk - 1;
-                            st_shared_u2(sa, (uint32_t)(r0 + 8 * ((x >> 1) & 1)), (uint32_t)(cb + 8 * (x >> 2) + (x & 1)));
+                            st_shared_u2(sa, cand_i(x), cand_j(x));
                             sa += 8;
                         }
                         fill += (uint32_t)total;

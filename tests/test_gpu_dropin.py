@@ -25,7 +25,8 @@ def harness(ctx):
 
 
 def run(harness, *args):
-    subprocess.run([harness] + [str(a) for a in args], check=True, capture_output=True, timeout=600)
+    r = subprocess.run([harness] + [str(a) for a in args], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, f"harness exited with {r.returncode}: {r.stderr[-2000:]}"
 
 
 def write_input(tmp_path, g):

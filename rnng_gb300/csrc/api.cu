@@ -24,11 +24,17 @@ float elapsed(rnng_ctx* c, int a, int b)
     return ms;
 }
 
+// Host points are copied to the context's buffer.  Device points are used in place when
+// they start on a 16-byte boundary (the kernels read rows with 16-byte loads and copies);
+// otherwise they are copied into the (aligned) buffer first.
 const float* upload_f32(rnng_ctx* c, DevBuf& buf, const float* X, int64_t count, unsigned flags)
 {
-    if (flags & RNNG_INPUT_DEVICE) return X;
+    const bool dev = flags & RNNG_INPUT_DEVICE;
+    if (dev && (count == 0 || ((uintptr_t)X & 15u) == 0)) return X;
     buf.reserve(sizeof(float) * (size_t)std::max<int64_t>(count, 1));
-    if (count) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, X, sizeof(float) * count, cudaMemcpyHostToDevice, c->stream));
+    if (count)
+        RNNG_CUDA(cudaMemcpyAsync(buf.ptr, X, sizeof(float) * count,
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
     return buf.as<float>();
 }
 

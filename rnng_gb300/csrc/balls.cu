@@ -441,18 +441,33 @@ __global__ void k_bitmap_pairs(const uint32_t* __restrict__ bitmap, int64_t S, i
     }
 }
 
+// Shared memory of the tensor-core pruning kernels: two buffers of a column block of 64
+// BF16 ball rows (padded by 64 bytes, so that the fragment reads of a quarter-warp, two
+// rows of four 16-byte columns, fall in distinct banks) and the balls' float4 terms.
+template <int KP>
+struct TileCloseSmem {
+    static constexpr int rowq = 4 * KP;         // uint4 per BF16 ball row (dp / 8)
+    static constexpr int srow = rowq + 4;       // staged row stride in uint4
+    static constexpr int buf = 64 * srow + 64;  // uint4 per buffer: 64 rows, then the balls' float4 terms
+    static constexpr size_t bytes = 2 * (size_t)buf * sizeof(uint4);
+};
+
 // Level 1 on the tensor cores (d <= 256): the same BF16 ball test as k_tile_close_mma
 // (below) over all pairs of super balls.  Block pairs (RB <= CB) of four super-tiles
 // (64 balls) each, taken as contiguous ranges of the row-major upper triangle per CUDA
 // block; warp w takes the 16 balls of row super-tile 4 RB + w against the 64 of the
 // column block, keeps the row block's A fragments in registers while RB lasts, and marks
 // super-tile pair (I, J), I <= J, in the S x S bitmap when any of its ball pairs passes.
+// The next pair's column block is staged in shared memory (cp.async) while the current
+// one is multiplied.
 template <int KP>
 __global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict__ cb, const float4* __restrict__ binfo,
                                                          int64_t S, float eps_p, float kappa,
                                                          uint32_t* __restrict__ bitmap)
 {
-    constexpr int rowq = 4 * KP;
+    using SM = TileCloseSmem<KP>;  // the same staging: a column block of 64 balls, two buffers
+    constexpr int rowq = SM::rowq, srow = SM::srow;
+    extern __shared__ uint4 ssm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
     const int64_t nR = (S + 3) / 4;
     const unsigned long long total = (unsigned long long)nR * (nR + 1) / 2;
@@ -473,15 +488,36 @@ __global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict
         first = row_first(RB);
     }
     int64_t CB = RB + (int64_t)(p0 - first);
+    // column block cbk into buffer bsel (one commit group)
+    auto stage = [&](int64_t cbk, int bsel) {
+        const int64_t rbb = cbk * 64;
+        const uint4* src = cb + rbb * rowq;
+        uint4* dst = ssm + bsel * SM::buf;
+        for (int i = threadIdx.x; i < 64 * rowq; i += blockDim.x) {
+            const int r = i / rowq, q = i - r * rowq;
+            cp_async16(dst + r * srow + q, src + i);
+        }
+        if (threadIdx.x < 64) cp_async16(dst + 64 * srow + threadIdx.x, binfo + rbb + threadIdx.x);
+        cp_async_commit();
+    };
     int64_t cur = -1;
     uint4 a0[KP], a1[KP];
     float4 x0 = make_float4(0.f, 0.f, 0.f, -1.f), x1 = x0;
+    stage(CB, 0);
     for (unsigned long long p = p0; p < p1; ++p) {
-        if (CB >= nR) {
-            ++RB;
-            CB = RB;
+        const int bsel = (int)((p - p0) & 1);
+        // the next pair's column block, staged while this pair is multiplied
+        const int64_t CBn = CB + 1 < nR ? CB + 1 : RB + 1;
+        if (p + 1 < p1) {
+            stage(CBn, bsel ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
-        const int64_t ra = RB * 64 + 16 * warp, rbb = CB * 64;
+        __syncthreads();
+        const uint4* bs = ssm + bsel * SM::buf;
+        const float4* ys = reinterpret_cast<const float4*>(bs + 64 * srow);
+        const int64_t ra = RB * 64 + 16 * warp;
         if (RB != cur) {
             const uint4* pa = cb + (ra + g) * rowq + t;
 #pragma unroll
@@ -498,12 +534,12 @@ __global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
-        const uint4* pb = cb + (rbb + g) * rowq + t;
+        const uint4* pb = bs + g * srow + t;
 #pragma unroll
         for (int kp = 0; kp < KP; ++kp) {
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) {
-                const uint4 b = pb[(8 * nt) * rowq + 4 * kp];
+                const uint4 b = pb[(8 * nt) * srow + 4 * kp];
                 mma_bf16_16816(acc[nt], a0[kp].x, a1[kp].x, a0[kp].y, a1[kp].y, b.x, b.y);
                 mma_bf16_16816(acc[nt], a0[kp].z, a1[kp].z, a0[kp].w, a1[kp].w, b.z, b.w);
             }
@@ -515,7 +551,7 @@ __global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const float4 y = binfo[rbb + 8 * nt + 2 * t + e];
+                const float4 y = ys[8 * nt + 2 * t + e];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float4 x = h ? x1 : x0;
@@ -535,7 +571,13 @@ __global__ void __launch_bounds__(128) k_super_close_mma(const uint4* __restrict
                 atomicOr(&bitmap[bit >> 5], 1u << (bit & 31));
             }
         }
-        ++CB;
+        if (CB + 1 < nR) {
+            ++CB;
+        } else {
+            ++RB;
+            CB = RB;
+        }
+        __syncthreads();  // every warp is done with buffer bsel before it is staged again
     }
 }
 
@@ -700,7 +742,9 @@ static_assert(kTileBalls == 8 && kSB == 64, "the warp layout of k_tile_close_mma
 
 // KP = dp / 32 k-groups.  Block b takes the contiguous range b of the super-pair list
 // (row-major, so consecutive pairs share their row super-tile) and keeps the row
-// super-tile's A fragments in registers while it lasts.
+// super-tile's A fragments in registers while it lasts.  The column super-tile's 64 ball
+// rows and their terms are staged in shared memory by cp.async, the next pair's while
+// the current one is multiplied.
 template <int KP>
 __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__ supers,
                                                         const unsigned long long* __restrict__ nsup_ptr,
@@ -709,17 +753,42 @@ __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__
                                                         float kappa, int2* __restrict__ out,
                                                         unsigned long long* __restrict__ count, unsigned long long cap)
 {
-    constexpr int rowq = 4 * KP;  // uint4 per BF16 row (dp / 8)
+    using SM = TileCloseSmem<KP>;
+    constexpr int rowq = SM::rowq, srow = SM::srow;
+    extern __shared__ uint4 tsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
     const unsigned long long nsup = min(*nsup_ptr, sup_cap);
     const unsigned long long per = (nsup + gridDim.x - 1) / gridDim.x;
     const unsigned long long w0 = (unsigned long long)blockIdx.x * per, w1 = min(nsup, w0 + per);
+    // the column super-tile of pair w into buffer bsel (one commit group)
+    auto stage = [&](unsigned long long w, int bsel) {
+        const int64_t rb = (int64_t)supers[w].y * kSB;
+        const uint4* src = cb + rb * rowq;
+        uint4* dst = tsm + bsel * SM::buf;
+        for (int i = threadIdx.x; i < kSB * rowq; i += blockDim.x) {
+            const int r = i / rowq, q = i - r * rowq;
+            cp_async16(dst + r * srow + q, src + i);
+        }
+        if (threadIdx.x < kSB) cp_async16(dst + kSB * srow + threadIdx.x, binfo + rb + threadIdx.x);
+        cp_async_commit();
+    };
     int cur = -1;
     uint4 a0[KP], a1[KP];
     float4 x0 = make_float4(0.f, 0.f, 0.f, -1.f), x1 = x0;
+    if (w0 < w1) stage(w0, 0);
     for (unsigned long long w = w0; w < w1; ++w) {
+        const int bsel = (int)((w - w0) & 1);
+        if (w + 1 < w1) {
+            stage(w + 1, bsel ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const uint4* bs = tsm + bsel * SM::buf;
+        const float4* ys = reinterpret_cast<const float4*>(bs + kSB * srow);
         const int2 sp = supers[w];
-        const int64_t ra = (int64_t)sp.x * kSB + 16 * warp, rb = (int64_t)sp.y * kSB;  // first ball rows
+        const int64_t ra = (int64_t)sp.x * kSB + 16 * warp;  // first row ball of this warp
         if (sp.x != cur) {
             const uint4* pa = cb + (ra + g) * rowq + t;
 #pragma unroll
@@ -736,12 +805,12 @@ __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
-        const uint4* pb = cb + (rb + g) * rowq + t;
+        const uint4* pb = bs + g * srow + t;
 #pragma unroll
         for (int kp = 0; kp < KP; ++kp) {
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) {
-                const uint4 b = pb[(8 * nt) * rowq + 4 * kp];
+                const uint4 b = pb[(8 * nt) * srow + 4 * kp];
                 mma_bf16_16816(acc[nt], a0[kp].x, a1[kp].x, a0[kp].y, a1[kp].y, b.x, b.y);
                 mma_bf16_16816(acc[nt], a0[kp].z, a1[kp].z, a0[kp].w, a1[kp].w, b.z, b.w);
             }
@@ -753,7 +822,7 @@ __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const float4 y = binfo[rb + 8 * nt + 2 * t + e];
+                const float4 y = ys[8 * nt + 2 * t + e];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float4 x = h ? x1 : x0;
@@ -771,14 +840,16 @@ __global__ void __launch_bounds__(128) k_tile_close_mma(const int2* __restrict__
         const int64_t j = (int64_t)sp.y * kSuper + (lane & 7);
         const bool mine = lane < 16 && ((msk >> lane) & 1u) && i < T && j < T && i <= j;
         const unsigned bal = __ballot_sync(0xffffffffu, mine);
-        if (!bal) continue;
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (mine) {
-            const unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
-            if (pos < cap) out[pos] = make_int2((int)i, (int)j);
+        if (bal) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (mine) {
+                const unsigned long long pos = base + __popc(bal & ((1u << lane) - 1u));
+                if (pos < cap) out[pos] = make_int2((int)i, (int)j);
+            }
         }
+        __syncthreads();  // every warp is done with buffer bsel before it is staged again
     }
 }
 
@@ -930,14 +1001,16 @@ void prune_covers(rnng_ctx* c, Layout& L)
         const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
         const int64_t nR = ceil_div(L.S, 4);
         const unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nR * (nR + 1) / 2, (int64_t)c->num_sms * 16));
-        auto launch = [&](auto kern) {
-            kern<<<sgrid, 128, 0, s>>>(c->sball_b16.as<uint4>(), c->sball_info.as<float4>(), L.S, eps_p, kappa, bitmap);
+        auto launch = [&](auto kern, size_t smem) {
+            RNNG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<sgrid, 128, smem, s>>>(c->sball_b16.as<uint4>(), c->sball_info.as<float4>(), L.S, eps_p, kappa,
+                                          bitmap);
         };
         switch (dp / 32) {
-            case 2: launch(k_super_close_mma<2>); break;
-            case 4: launch(k_super_close_mma<4>); break;
-            case 6: launch(k_super_close_mma<6>); break;
-            default: launch(k_super_close_mma<8>); break;
+            case 2: launch(k_super_close_mma<2>, TileCloseSmem<2>::bytes); break;
+            case 4: launch(k_super_close_mma<4>, TileCloseSmem<4>::bytes); break;
+            case 6: launch(k_super_close_mma<6>, TileCloseSmem<6>::bytes); break;
+            default: launch(k_super_close_mma<8>, TileCloseSmem<8>::bytes); break;
         }
         ++c->launches;
     } else {
@@ -988,16 +1061,17 @@ void prune_covers(rnng_ctx* c, Layout& L)
         const float kappa = 1.0f / (1 << 20);  // relative slack for the FP32 evaluation of the test
         const unsigned wgrid = (unsigned)std::max<unsigned long long>(
             1, std::min<unsigned long long>(L.super_pairs, (unsigned long long)c->num_sms * 16));
-        auto launch = [&](auto kern) {
-            kern<<<wgrid, 128, 0, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->ball_b16.as<uint4>(),
-                                       c->ball_info.as<float4>(), L.T, eps_p, kappa, c->pair_list.as<int2>(), cnt + 1,
-                                       tile_cap);
+        auto launch = [&](auto kern, size_t smem) {
+            RNNG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<wgrid, 128, smem, s>>>(c->super_list.as<int2>(), cnt, L.super_pairs, c->ball_b16.as<uint4>(),
+                                          c->ball_info.as<float4>(), L.T, eps_p, kappa, c->pair_list.as<int2>(),
+                                          cnt + 1, tile_cap);
         };
         switch (dp / 32) {
-            case 2: launch(k_tile_close_mma<2>); break;
-            case 4: launch(k_tile_close_mma<4>); break;
-            case 6: launch(k_tile_close_mma<6>); break;
-            default: launch(k_tile_close_mma<8>); break;
+            case 2: launch(k_tile_close_mma<2>, TileCloseSmem<2>::bytes); break;
+            case 4: launch(k_tile_close_mma<4>, TileCloseSmem<4>::bytes); break;
+            case 6: launch(k_tile_close_mma<6>, TileCloseSmem<6>::bytes); break;
+            default: launch(k_tile_close_mma<8>, TileCloseSmem<8>::bytes); break;
         }
         ++c->launches;
     } else {

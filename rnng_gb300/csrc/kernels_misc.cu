@@ -96,9 +96,14 @@ void sort_edges_uv(rnng_ctx* c, int64_t* u, int64_t* v, float* w, int64_t m, boo
 
 const void* upload(rnng_ctx* c, DevBuf& buf, const void* p, size_t bytes, unsigned flags)
 {
-    if (!p || (flags & RNNG_INPUT_DEVICE)) return p;
+    // device data off a 16-byte boundary is copied, so that the kernels' 16-byte loads and
+    // copies stay aligned
+    const bool dev = flags & RNNG_INPUT_DEVICE;
+    if (!p || (dev && (bytes == 0 || ((uintptr_t)p & 15u) == 0))) return p;
     buf.reserve(std::max<size_t>(bytes, 1));
-    if (bytes) RNNG_CUDA(cudaMemcpyAsync(buf.ptr, p, bytes, cudaMemcpyHostToDevice, c->stream));
+    if (bytes)
+        RNNG_CUDA(cudaMemcpyAsync(buf.ptr, p, bytes, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream));
     return buf.ptr;
 }
 

@@ -271,3 +271,26 @@ def test_gram_tuning_table_and_override(ctx, orc):
     ctx.set_gram_tuning(0, 0, 0)
     ctx.eps_graph_l2(x, r, mode="bf16")
     assert (ctx.stats()["gram_nt"], ctx.stats()["gram_chunk"]) == (row["nt"], row["chunk"])
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("d", [32, 128])
+def test_device_points_off_16_byte_boundary(ctx, orc, mode, d):
+    """Device points that start 4 bytes past a 16-byte boundary (a view into a larger
+    buffer) give the oracle's edges: the library copies them to an aligned buffer before
+    its 16-byte loads (host-side result, INPUT_DEVICE only)."""
+    torch = pytest.importorskip("torch")
+    import rnng_gb300
+    rng = np.random.default_rng(40 + d)
+    n = 1500
+    centres = rng.uniform(-10, 10, size=(8, d))
+    x = (centres[rng.integers(0, 8, n)] + rng.normal(size=(n, d))).astype(np.float32)
+    r = np.float32(1.6 * np.sqrt(d))
+    want = orc.eps_graph_l2(x, r)
+    buf = torch.zeros(n * d + 1, dtype=torch.float32, device="cuda")
+    buf[1:] = torch.from_numpy(x.reshape(-1)).cuda()
+    xd = buf[1:]
+    assert xd.data_ptr() % 16 == 4
+    e = ctx.eps_graph_l2_raw(xd.data_ptr(), None, n, d, r, rnng_gb300.MODES[mode],
+                             rnng_gb300.INPUT_DEVICE | rnng_gb300.SORT_OUTPUT)
+    assert same(ctx._edges_out(e), want)

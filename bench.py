@@ -371,9 +371,12 @@ def main():
         t_e2e.append(time.perf_counter() - t0)
         assert e.count == edges
     e2e_s = statistics.median(t_e2e)
+    st_e2e = ctx.stats()  # the last end-to-end call's copy times (CUDA events on the library's stream)
     err64 = fp64_error(x, *ctx._edges_out(e)) if rank == 0 else None
     e2e = {"value": world * edges / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(n * d * 4),
-           "d2h_bytes_per_step": int(edges * (8 + 8 + 4)), "ms_per_step": e2e_s * 1e3}
+           "d2h_bytes_per_step": int(edges * (8 + 8 + 4)), "ms_per_step": e2e_s * 1e3,
+           "ms_h2d": round(st_e2e["ms_h2d"], 3), "ms_d2h": round(st_e2e["ms_d2h"], 3),
+           "ms_device_total": round(st_e2e["ms_total"], 3)}
 
     # ---- roofline of the dominant kernel (tcgen05 Gram tiles)
     burst, sustained, src = peaks_bf16()

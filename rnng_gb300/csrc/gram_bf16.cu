@@ -1242,6 +1242,67 @@ __global__ void __launch_bounds__(256) k_colsum(const float* __restrict__ Xs, in
     }
 }
 
+// The same sums for d a multiple of 4: each thread adds four consecutive dimensions from
+// 16-byte loads, four rows per round in flight (the scalar form left HBM latency exposed:
+// 3 TB/s at 1M x 128).
+__global__ void __launch_bounds__(256) k_colsum4(const float* __restrict__ Xs, int64_t n, int d,
+                                                 double* __restrict__ sums, unsigned long long* __restrict__ screen)
+{
+    __shared__ float4 part[256];
+    const int nq = d >> 2;      // float4 per row (d <= 256: at most 64)
+    const int rps = 256 / nq;   // rows per step
+    const int t = threadIdx.x;
+    const bool active = t < rps * nq;
+    const int q = t % nq;
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float mx = 0.f;
+    bool bad = false;
+    auto add = [&](const float4 v) {
+        bad |= nonfinite_f32(v.x) | nonfinite_f32(v.y) | nonfinite_f32(v.z) | nonfinite_f32(v.w);
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+        acc.x += v.x;
+        acc.y += v.y;
+        acc.z += v.z;
+        acc.w += v.w;
+    };
+    if (active) {
+        const float4* X4 = reinterpret_cast<const float4*>(Xs);
+        int64_t r = r0 + t / nq;
+        for (; r + 3 * rps < r1; r += 4 * rps) {
+            const float4 a = __ldg(X4 + r * nq + q), b = __ldg(X4 + (r + rps) * nq + q);
+            const float4 c = __ldg(X4 + (r + 2 * rps) * nq + q), e = __ldg(X4 + (r + 3 * rps) * nq + q);
+            add(a);
+            add(b);
+            add(c);
+            add(e);
+        }
+        for (; r < r1; r += rps) add(__ldg(X4 + r * nq + q));
+    }
+    part[t] = acc;
+    if (screen) {
+        // non-negative floats order as their bit patterns
+        const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(mx));
+        if ((t & 31) == 0 && m) atomicMax(&screen[1], (unsigned long long)m);
+    }
+    if (__syncthreads_or(bad) && screen && t == 0) screen[0] = 1ull;
+    if (t < nq && r0 < r1) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        for (int k = 0; k < rps; ++k) {
+            const float4 p = part[k * nq + t];
+            s0 += (double)p.x;
+            s1 += (double)p.y;
+            s2 += (double)p.z;
+            s3 += (double)p.w;
+        }
+        atomicAdd(&sums[4 * t], s0);
+        atomicAdd(&sums[4 * t + 1], s1);
+        atomicAdd(&sums[4 * t + 2], s2);
+        atomicAdd(&sums[4 * t + 3], s3);
+    }
+}
+
 // Rounded column means.  A non-finite column sum (a NaN or infinite coordinate, or a
 // float partial that overflowed) gets shift 0: any finite shift keeps the BF16 error
 // bounds valid.
@@ -1291,6 +1352,51 @@ __device__ __forceinline__ float3 bf16_row(const float* __restrict__ x, bool rea
     return make_float3(nrm, a, q);
 }
 
+// bf16_row for d a multiple of 4 and x on a 16-byte boundary: lane l takes columns 4 l ..
+// 4 l + 3 (then 4 l + 128 ..), one 16-byte load and one 8-byte store each; outB, when
+// given, receives the same row (zeros past d).  Same terms as bf16_row, summed in another
+// order (the bounds hold for any order of the FP32 sums).
+__device__ __forceinline__ float3 bf16_row4(const float* __restrict__ x, bool real, int d, int dp,
+                                            const float* __restrict__ shift, float gamma,
+                                            __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ outB)
+{
+    const int lane = threadIdx.x & 31;
+    const float u = 5.9604644775390625e-08f;  // 2^-24
+    float nrm = 0.f, res = 0.f, xc = 0.f;
+    for (int k = 4 * lane; k < dp; k += 128) {
+        float b[4] = {0.f, 0.f, 0.f, 0.f};
+        if (real && k < d) {
+            const float4 xv = *reinterpret_cast<const float4*>(x + k);
+            const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float t = __fsub_rn(xs[j], shift[k + j]);
+                b[j] = __bfloat162float(__float2bfloat16_rn(t));
+                const float e = __fsub_rn(t, b[j]);  // exact: b is t rounded to 8 bits
+                nrm = fmaf(b[j], b[j], nrm);
+                res = fmaf(e, e, res);
+                xc = fmaf(t, t, xc);
+            }
+        }
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(b[0], b[1]), hi = __floats2bfloat162_rn(b[2], b[3]);
+        uint2 pk;
+        pk.x = *reinterpret_cast<const uint32_t*>(&lo);
+        pk.y = *reinterpret_cast<const uint32_t*>(&hi);
+        *reinterpret_cast<uint2*>(out + k) = pk;
+        if (outB) *reinterpret_cast<uint2*>(outB + k) = pk;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+        res += __shfl_xor_sync(0xffffffffu, res, o);
+        xc += __shfl_xor_sync(0xffffffffu, xc, o);
+    }
+    const float grow = 1.f + (float)(d + 8) * u;
+    const float a = (sqrtf(res) + u * sqrtf(xc)) * grow * grow + 1e-30f;
+    const float q = gamma * nrm * grow;
+    return make_float3(nrm, a, q);
+}
+
 // One warp per sorted row: BF16 operand row (dp columns, zero padded) and the
 // row's {norm, error radius, Gram error term, norm - a^2 - q} for the candidate test.
 // With fold (dp >= d + 4) the row is written twice: as a row-tile operand (Xb) with
@@ -1307,12 +1413,19 @@ __global__ void k_to_bf16(const float* __restrict__ Xs, int64_t n, int64_t n_pad
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
+    const bool vec = (d & 3) == 0;  // rows on 16-byte boundaries
     for (int64_t r = warp; r < n_pad; r += nwarps) {
-        const float3 v = bf16_row(Xs + r * d, r < n, d, dp, shift, gamma, Xb + r * dp);
-        if (fold) {
-            // the same row as a column-tile operand (padding written below)
-            for (int k = lane; k < d; k += 32) XbB[r * dp + k] = Xb[r * dp + k];
-            for (int k = d + 4 + lane; k < dp; k += 32) XbB[r * dp + k] = __float2bfloat16_rn(0.f);
+        float3 v;
+        if (vec) {
+            // the row-tile and (fold) column-tile operands together; columns d .. d + 3 below
+            v = bf16_row4(Xs + r * d, r < n, d, dp, shift, gamma, Xb + r * dp, fold ? XbB + r * dp : nullptr);
+        } else {
+            v = bf16_row(Xs + r * d, r < n, d, dp, shift, gamma, Xb + r * dp);
+            if (fold) {
+                // the same row as a column-tile operand (padding written below)
+                for (int k = lane; k < d; k += 32) XbB[r * dp + k] = Xb[r * dp + k];
+                for (int k = d + 4 + lane; k < dp; k += 32) XbB[r * dp + k] = __float2bfloat16_rn(0.f);
+            }
         }
         __syncwarp();  // the zeros other lanes wrote to columns d .. d + 3 come first
         if (lane == 0) {
@@ -1439,7 +1552,12 @@ const float* bf16_shift(rnng_ctx* c, Layout& L, const float* X, unsigned long lo
     RNNG_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * d, s));
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 4));
     if (screen) RNNG_CUDA(cudaMemsetAsync(screen, 0, 2 * sizeof(unsigned long long), s));
-    k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums, screen); ++c->launches;
+    if ((d & 3) == 0)
+        k_colsum4<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(L.n, 512), (int64_t)c->num_sms * 8)), 256,
+                    0, s>>>(X, L.n, d, sums, screen);
+    else
+        k_colsum<<<(unsigned)blocks, 256, 0, s>>>(X, L.n, d, sums, screen);
+    ++c->launches;
     k_shift<<<1, 256, 0, s>>>(sums, L.n, d, shift); ++c->launches;
     L.shift = shift;
     return shift;

@@ -306,11 +306,17 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
     __syncthreads();
 }
 
+// Row stride of a staged tile: d + 4 floats when d is a multiple of 4 (rows on 16-byte
+// boundaries, so the distance walks read 16 bytes at a time, and the eight rows of a
+// quarter-warp's 16-byte reads four banks apart), else d + 1 (the threads' row walks in
+// distinct banks).
+__host__ __device__ constexpr int tile_row_stride(int d) { return (d & 3) == 0 ? d + 4 : d + 1; }
+
 // One block per tile.  Output: centres [T][kTileBalls][d], radii [T][kTileBalls] (-1 =
 // unused).  With staged = true the tile's rows are first copied to shared memory (rows
-// d + 1 floats apart, so that the threads' row walks hit distinct banks), which every
-// pass of the greedy then reads.  Dynamic shared memory: d floats (centroid), kTileBalls d
-// floats with use_sums (group sums), and kTile (d + 1) floats when staged.
+// tile_row_stride(d) floats apart), which every pass of the greedy then reads.  Dynamic
+// shared memory: d floats (centroid), kTileBalls d floats with use_sums (group sums), and
+// kTile tile_row_stride(d) floats when staged.
 __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d,
                                                               float grow, bool staged, bool use_sums,
                                                               float* __restrict__ cen, float* __restrict__ rad)
@@ -327,23 +333,18 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
     int ld = d;
     if (staged) {
         const int total = nitems * d;
+        ld = tile_row_stride(d);
         if ((d & 3) == 0) {
             const float4* s4 = reinterpret_cast<const float4*>(src);
             for (int i = threadIdx.x; i < total / 4; i += blockDim.x) {
-                const float4 v = __ldg(s4 + i);
                 const int r = (4 * i) / d, k = (4 * i) % d;  // d % 4 == 0: the four stay in row r
-                float* dst = tile_rows + r * (d + 1) + k;
-                dst[0] = v.x;
-                dst[1] = v.y;
-                dst[2] = v.z;
-                dst[3] = v.w;
+                *reinterpret_cast<float4*>(tile_rows + r * ld + k) = __ldg(s4 + i);
             }
         } else {
-            for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[(i / d) * (d + 1) + i % d] = __ldg(src + i);
+            for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[(i / d) * ld + i % d] = __ldg(src + i);
         }
         __syncthreads();
         src = tile_rows;
-        ld = d + 1;
     }
     cover_groups(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, use_sums ? sums : nullptr,
                  cen + t * kTileBalls * d, rad + t * kTileBalls);
@@ -947,7 +948,7 @@ void build_covers(rnng_ctx* c, Layout& L)
     const bool tsums = (size_t)kTileBalls * L.d * sizeof(float) <= 32768;
     const bool ssums = (size_t)kSuperBalls * L.d * sizeof(float) <= 32768;
     const size_t tsm = csm + (tsums ? sizeof(float) * kTileBalls * (size_t)L.d : 0) +
-                       (staged ? sizeof(float) * kTile * (size_t)(L.d + 1) : 0);
+                       (staged ? sizeof(float) * kTile * (size_t)tile_row_stride(L.d) : 0);
     const size_t ssm = csm + (ssums ? sizeof(float) * kSuperBalls * (size_t)L.d : 0);
     RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));

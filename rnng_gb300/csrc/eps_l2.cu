@@ -99,6 +99,24 @@ __global__ void k_gather_sorted(const float* __restrict__ X, int64_t n, int64_t 
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    if (d == 128) {
+        // the common width: four rows per warp and round, their loads in flight together
+        for (int64_t r = warp; r < n_pad; r += 4 * nwarps) {
+            float4 v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t rj = r + j * nwarps;
+                v[j] = rj < n ? __ldg(reinterpret_cast<const float4*>(X + (int64_t)perm[rj] * d) + lane)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int64_t rj = r + j * nwarps;
+                if (rj < n_pad) reinterpret_cast<float4*>(Xs + rj * d)[lane] = v[j];
+            }
+        }
+        return;
+    }
     for (int64_t r = warp; r < n_pad; r += nwarps) {
         float* dst = Xs + r * d;
         const float* src = r < n ? X + (int64_t)perm[r] * d : nullptr;

@@ -351,7 +351,8 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
 }
 
 // One block per super-tile: kSuperBalls balls over its tiles' valid balls (items with
-// their radii).  Dynamic shared memory: d floats, plus kSuperBalls d with use_sums.
+// their radii).  Dynamic shared memory: d floats, plus kSuperBalls d with use_sums, plus
+// the staged ball centres (64 (d + 4) floats) when d is a multiple of 4 up to 128.
 __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __restrict__ tcen,
                                                                const float* __restrict__ trad, int64_t T, int d,
                                                                float grow, bool use_sums, float* __restrict__ work,
@@ -360,30 +361,53 @@ __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __re
     __shared__ CoverState st;
     __shared__ float irad[kSuper * kTileBalls];
     __shared__ int src_ball[kSuper * kTileBalls];
-    __shared__ int nvalid;
+    __shared__ int wcount[kCoverThreads / 32];
     extern __shared__ __align__(16) float dsm[];
+    static_assert(kCoverThreads >= kSuper * kTileBalls, "one thread per tile ball of the super-tile");
     const int64_t s = blockIdx.x;
     const int64_t t0 = s * kSuper, t1 = min(T, t0 + kSuper);
-    float* items = work + s * (int64_t)kSuper * kTileBalls * d;  // compacted valid ball centres
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int64_t t = t0; t < t1; ++t)
-            for (int k = 0; k < kTileBalls; ++k)
-                if (trad[t * kTileBalls + k] >= 0.f) {
-                    irad[m] = trad[t * kTileBalls + k];
-                    src_ball[m] = (int)((t - t0) * kTileBalls + k);
-                    ++m;
-                }
-        nvalid = m;
+    // the valid tile balls, compacted in ball order (ballot and warp counts)
+    const int bi = threadIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool valid = bi < (int)(t1 - t0) * kTileBalls && trad[t0 * kTileBalls + bi] >= 0.f;
+    const unsigned bal = __ballot_sync(0xffffffffu, valid);
+    if (lane == 0) wcount[warp] = __popc(bal);
+    __syncthreads();
+    int pos = __popc(bal & ((1u << lane) - 1u)), m = 0;
+    for (int w = 0; w < kCoverThreads / 32; ++w) {
+        if (w < warp) pos += wcount[w];
+        m += wcount[w];
+    }
+    if (valid) {
+        irad[pos] = trad[t0 * kTileBalls + bi];
+        src_ball[pos] = bi;
     }
     __syncthreads();
-    const int m = nvalid;
-    for (int i = 0; i < m; ++i)
-        for (int j = threadIdx.x; j < d; j += blockDim.x)
-            items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
+    float* cbuf = dsm;
+    float* sums = use_sums ? dsm + ((d + 3) & ~3) : nullptr;
+    // their centres: staged in shared memory 16 bytes at a time (rows d + 4 floats apart)
+    // when d is a multiple of 4 and at most 128, else compacted in the global workspace
+    const bool staged = (d & 3) == 0 && d <= 128;
+    float* items;
+    int ld;
+    if (staged) {
+        items = dsm + ((d + 3) & ~3) + (use_sums ? kSuperBalls * d : 0);
+        ld = d + 4;
+        const int nq = d >> 2;
+        const float4* c4 = reinterpret_cast<const float4*>(tcen);
+        for (int e = threadIdx.x; e < m * nq; e += blockDim.x) {
+            const int i = e / nq, q = e - i * nq;
+            *reinterpret_cast<float4*>(items + i * ld + 4 * q) = __ldg(c4 + (t0 * kTileBalls + src_ball[i]) * nq + q);
+        }
+    } else {
+        items = work + s * (int64_t)kSuper * kTileBalls * d;
+        ld = d;
+        for (int i = 0; i < m; ++i)
+            for (int j = threadIdx.x; j < d; j += blockDim.x)
+                items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
+    }
     __syncthreads();
-    cover_groups(st, items, d, irad, m, d, kSuperBalls, grow, dsm, use_sums ? dsm + ((d + 3) & ~3) : nullptr,
-                 scen + s * kSuperBalls * d, srad + s * kSuperBalls);
+    cover_groups(st, items, ld, irad, m, d, kSuperBalls, grow, cbuf, sums, scen + s * kSuperBalls * d,
+                 srad + s * kSuperBalls);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -949,7 +973,8 @@ void build_covers(rnng_ctx* c, Layout& L)
     const bool ssums = (size_t)kSuperBalls * L.d * sizeof(float) <= 32768;
     const size_t tsm = csm + (tsums ? sizeof(float) * kTileBalls * (size_t)L.d : 0) +
                        (staged ? sizeof(float) * kTile * (size_t)tile_row_stride(L.d) : 0);
-    const size_t ssm = csm + (ssums ? sizeof(float) * kSuperBalls * (size_t)L.d : 0);
+    const size_t ssm = csm + (ssums ? sizeof(float) * kSuperBalls * (size_t)L.d : 0) +
+                       ((L.d & 3) == 0 && L.d <= 128 ? sizeof(float) * kSuper * kTileBalls * (size_t)(L.d + 4) : 0);
     RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
     RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
     k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, tsums,

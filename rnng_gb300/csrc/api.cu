@@ -68,7 +68,7 @@ int64_t tiles_with_retry(rnng_ctx* c, Layout& L, int mode, EdgeOut& E)
         RNNG_CUDA(cudaMemcpyAsync(&got, E.count, sizeof(got), cudaMemcpyDeviceToHost, c->stream));
         RNNG_CUDA(cudaStreamSynchronize(c->stream));
         check_device_fault(c);
-        if (got <= cap) {
+        if (got <= E.cap) {  // (the direct output sizes E.cap to the candidates)
             c->edge_cap_hint = std::max<unsigned long long>(c->edge_cap_hint, got + got / 8);
             return (int64_t)got;
         }
@@ -76,6 +76,35 @@ int64_t tiles_with_retry(rnng_ctx* c, Layout& L, int mode, EdgeOut& E)
         cap = got + got / 8 + 1024;
         c->stats.retries++;
     }
+}
+
+
+// Stage times (CUDA events 0..10 of the call) and counts of an epsilon-graph call.
+void record_eps_stats(rnng_ctx* c, const Layout& L, int mode, int64_t m)
+{
+    rnng_stats& st = c->stats;
+    st.ms_h2d = elapsed(c, 0, 1);
+    st.ms_partition = elapsed(c, 1, 2);
+    st.ms_bounds = elapsed(c, 2, 3);
+    st.ms_prune = elapsed(c, 3, 4);
+    if (mode == RNNG_MODE_BF16_RECHECK) {
+        st.ms_tiles = elapsed(c, 4, 8);
+        st.ms_recheck = elapsed(c, 8, 5);
+    } else {
+        st.ms_tiles = elapsed(c, 4, 5);
+    }
+    st.ms_finalize = elapsed(c, 5, 6);
+    st.ms_d2h = elapsed(c, 6, 7);
+    st.ms_total = elapsed(c, 0, 7);
+    st.num_cells = L.num_cells;
+    st.super_pairs = (int64_t)L.super_pairs;
+    st.tile_pairs = (int64_t)L.tile_pairs;
+    st.tile_pairs_all = L.T * (L.T + 1) / 2;
+    st.pairs_evaluated = (int64_t)L.tile_pairs * kTile * kTile;
+    st.edges = m;
+    st.candidates = c->last_candidates;
+    st.kernel_launches = c->launches;
+    st.ms_gram = c->gram_ms;
 }
 
 }  // namespace
@@ -113,6 +142,8 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
         }
         L = build_layout(c, Xf, n, d, radius, false);
     }
+    // sorted position -> input row from here on (the direct output maps through it)
+    if (remap) remap_rows(c, L.perm, n, n_in);
     RNNG_CUDA(cudaEventRecord(c->ev[2], s));
     build_covers(c, L);
     RNNG_CUDA(cudaEventRecord(c->ev[3], s));
@@ -133,9 +164,10 @@ int64_t eps_core(rnng_ctx* c, const float* dX, int64_t n, int d, float radius, i
         schedule_items(c, L, t.nt);
         prepare_bf16(c, L);
     }
+    E.perm = L.perm;
+    if (tmode != RNNG_MODE_BF16_RECHECK) E.direct = false;  // the FP32-direct tiles write sorted positions
     const int64_t m = tiles_with_retry(c, L, tmode, E);
     if (tmode != mode) RNNG_CUDA(cudaEventRecord(c->ev[8], s));
-    if (remap) remap_rows(c, L.perm, n, n_in);
     RNNG_CUDA(cudaEventRecord(c->ev[5], s));
     return m;
 }
@@ -276,7 +308,24 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         }
         Layout L;
         EdgeOut E;
+        // host results in any order: the recheck writes them to the pinned staging block itself
+        E.direct = !(flags & (RNNG_OUTPUT_DEVICE | RNNG_SORT_OUTPUT)) && mode == RNNG_MODE_BF16_RECHECK;
+        E.ids = dids;
         const int64_t m = eps_core(c, dX, n, (int)d, radius, mode, L, E);
+        if (E.direct && E.hu) {
+            RNNG_CUDA(cudaEventRecord(c->ev[6], s));
+            std::memset(out, 0, sizeof(*out));
+            out->count = m;
+            out->staged = 1;
+            out->u = E.hu;
+            out->v = E.hv;
+            out->w = E.hw;
+            RNNG_CUDA(cudaEventRecord(c->ev[7], s));
+            RNNG_CUDA(cudaStreamSynchronize(s));
+            RNNG_CUDA(cudaGetLastError());
+            record_eps_stats(c, L, mode, m);
+            return;
+        }
         c->out_u.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
         c->out_v.reserve(sizeof(int64_t) * std::max<int64_t>(m, 1));
         c->out_w.reserve(sizeof(float) * std::max<int64_t>(m, 1));
@@ -288,29 +337,7 @@ int rnng_eps_graph_l2(rnng_ctx* c, const float* X, const int64_t* ids, int64_t n
         RNNG_CUDA(cudaEventRecord(c->ev[7], s));
         RNNG_CUDA(cudaStreamSynchronize(s));
         RNNG_CUDA(cudaGetLastError());
-        rnng_stats& st = c->stats;
-        st.ms_h2d = elapsed(c, 0, 1);
-        st.ms_partition = elapsed(c, 1, 2);
-        st.ms_bounds = elapsed(c, 2, 3);
-        st.ms_prune = elapsed(c, 3, 4);
-        if (mode == RNNG_MODE_BF16_RECHECK) {
-            st.ms_tiles = elapsed(c, 4, 8);
-            st.ms_recheck = elapsed(c, 8, 5);
-        } else {
-            st.ms_tiles = elapsed(c, 4, 5);
-        }
-        st.ms_finalize = elapsed(c, 5, 6);
-        st.ms_d2h = elapsed(c, 6, 7);
-        st.ms_total = elapsed(c, 0, 7);
-        st.num_cells = L.num_cells;
-        st.super_pairs = (int64_t)L.super_pairs;
-        st.tile_pairs = (int64_t)L.tile_pairs;
-        st.tile_pairs_all = L.T * (L.T + 1) / 2;
-        st.pairs_evaluated = (int64_t)L.tile_pairs * kTile * kTile;
-        st.edges = m;
-        st.candidates = c->last_candidates;
-        st.kernel_launches = c->launches;
-        st.ms_gram = c->gram_ms;
+        record_eps_stats(c, L, mode, m);
     });
 }
 

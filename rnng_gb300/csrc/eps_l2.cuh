@@ -55,6 +55,44 @@ struct EdgeOut {
     float* w = nullptr;
     unsigned long long* count = nullptr;  // device counter
     unsigned long long cap = 0;
+    // Direct output (BF16 tiles, host results, no sorting): the recheck writes each edge as
+    // (input id u < v, weight) straight into the context's pinned staging block through its
+    // device address, so the results cross to the host while the recheck runs.  `direct`
+    // is the request; run_tiles_bf16 clears it when it cannot honour it, else sets the host
+    // arrays (room for every candidate) and cap.
+    bool direct = false;
+    const int32_t* perm = nullptr;  // sorted position -> input row
+    const int64_t* ids = nullptr;   // input row -> id (nullptr: the row itself)
+    int64_t* hu = nullptr;
+    int64_t* hv = nullptr;
+    float* hw = nullptr;
+};
+
+// Where the recheck puts an edge: its sorted positions into the pipeline's edge list, or,
+// with du set, the final (input id u < v, weight) through perm and ids.
+struct EdgeSink {
+    uint32_t* eu = nullptr;
+    uint32_t* ev = nullptr;
+    float* ew = nullptr;
+    int64_t* du = nullptr;
+    int64_t* dv = nullptr;
+    float* dw = nullptr;
+    const int32_t* perm = nullptr;
+    const int64_t* ids = nullptr;
+    __device__ __forceinline__ void put(unsigned long long pos, uint32_t i, uint32_t j, float w) const
+    {
+        if (du) {
+            const int32_t a = perm[i], b = perm[j];
+            const int64_t ia = ids ? ids[a] : (int64_t)a, ib = ids ? ids[b] : (int64_t)b;
+            du[pos] = ia < ib ? ia : ib;
+            dv[pos] = ia < ib ? ib : ia;
+            dw[pos] = w;
+        } else {
+            eu[pos] = i;
+            ev[pos] = j;
+            ew[pos] = w;
+        }
+    }
 };
 
 // screen: first test the input for NaN or infinite values (fused into the BF16 column

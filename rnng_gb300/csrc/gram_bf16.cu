@@ -1058,8 +1058,7 @@ __global__ void __maxnreg__(kGramMaxRegs)
 // rows are a few cache lines each).
 __global__ void __launch_bounds__(256) k_recheck_direct(const float* __restrict__ Xs, int d, const uint2* __restrict__ cand,
                                                  const unsigned long long* __restrict__ ncand_ptr,
-                                                 unsigned long long cand_cap, float radius, uint32_t* __restrict__ eu,
-                                                 uint32_t* __restrict__ ev, float* __restrict__ ew,
+                                                 unsigned long long cand_cap, float radius, const EdgeSink sink,
                                                  unsigned long long* __restrict__ ecount, unsigned long long cap)
 {
     __shared__ int s_warp[8];
@@ -1105,11 +1104,7 @@ __global__ void __launch_bounds__(256) k_recheck_direct(const float* __restrict_
         __syncthreads();
         if (hit) {
             const unsigned long long pos = s_base + s_warp[warp] + __popc(ball & ((1u << lane) - 1u));
-            if (pos < cap) {
-                eu[pos] = c.x;
-                ev[pos] = c.y;
-                ew[pos] = w;
-            }
+            if (pos < cap) sink.put(pos, c.x, c.y, w);
         }
         __syncthreads();
     }
@@ -1127,8 +1122,7 @@ __global__ void __launch_bounds__(32 * kRecheckWarps) k_recheck(const float* __r
                                                                 const uint2* __restrict__ cand,
                                                                 const unsigned long long* __restrict__ ncand_ptr,
                                                                 unsigned long long cand_cap, float radius,
-                                                                uint32_t* __restrict__ eu, uint32_t* __restrict__ ev,
-                                                                float* __restrict__ ew,
+                                                                const EdgeSink sink,
                                                                 unsigned long long* __restrict__ ecount,
                                                                 unsigned long long cap)
 {
@@ -1192,11 +1186,7 @@ __global__ void __launch_bounds__(32 * kRecheckWarps) k_recheck(const float* __r
         __syncthreads();
         if (hit) {
             const unsigned long long pos = s_base + s_warp[warp] + __popc(ball & ((1u << lane) - 1u));
-            if (pos < cap) {
-                eu[pos] = c.x;
-                ev[pos] = c.y;
-                ew[pos] = w;
-            }
+            if (pos < cap) sink.put(pos, c.x, c.y, w);
         }
         __syncthreads();
     }
@@ -1879,17 +1869,40 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
     const unsigned long long ccap = std::max<unsigned long long>(1u << 20, c->cand_cap_hint);
     RNNG_CUDA(cudaEventRecord(c->ev[8], s));
     const unsigned long long ncand = (unsigned long long)c->last_candidates;
+    EdgeSink sink;
+    sink.eu = E.si;
+    sink.ev = E.sj;
+    sink.ew = E.w;
+    if (E.direct) {
+        // every candidate can be an edge: room for all of them in the pinned staging block,
+        // written through its device address
+        const unsigned long long cap = std::max<unsigned long long>(ncand, 1);
+        char* h = (char*)host_stage(c, (size_t)cap * (2 * sizeof(int64_t) + sizeof(float)));
+        void* dptr = nullptr;
+        if (cudaHostGetDevicePointer(&dptr, h, 0) == cudaSuccess && dptr) {
+            E.hu = reinterpret_cast<int64_t*>(h);
+            E.hv = E.hu + cap;
+            E.hw = reinterpret_cast<float*>(E.hv + cap);
+            sink.du = reinterpret_cast<int64_t*>(dptr);
+            sink.dv = sink.du + cap;
+            sink.dw = reinterpret_cast<float*>(sink.dv + cap);
+            sink.perm = E.perm;
+            sink.ids = E.ids;
+            E.cap = cap;
+        } else {
+            (void)cudaGetLastError();  // no device address for the staging block: the usual path
+            E.direct = false;
+        }
+    }
     const int rthreads = 32 * kRecheckWarps;
     const int rgrid = (int)std::max<unsigned long long>(
         1, std::min<unsigned long long>((ncand + rthreads - 1) / rthreads, (unsigned long long)c->num_sms * 16));
     if ((L.d & 31) == 0)
-        k_recheck<<<rgrid, rthreads, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w,
-                                             E.count, E.cap);
+        k_recheck<<<rgrid, rthreads, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, sink, E.count, E.cap);
     else
         k_recheck_direct<<<(int)std::max<unsigned long long>(
                                1, std::min<unsigned long long>((ncand + 255) / 256, (unsigned long long)c->num_sms * 8)),
-                           256, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, E.si, E.sj, E.w, E.count,
-                                        E.cap);
+                           256, 0, s>>>(L.Xs, L.d, c->cand.as<uint2>(), cnt, ccap, L.radius, sink, E.count, E.cap);
     ++c->launches;
     RNNG_CUDA(cudaGetLastError());
 }

@@ -294,3 +294,30 @@ def test_device_points_off_16_byte_boundary(ctx, orc, mode, d):
     e = ctx.eps_graph_l2_raw(xd.data_ptr(), None, n, d, r, rnng_gb300.MODES[mode],
                              rnng_gb300.INPUT_DEVICE | rnng_gb300.SORT_OUTPUT)
     assert same(ctx._edges_out(e), want)
+
+
+@pytest.mark.parametrize("d", [33, 128])
+@pytest.mark.parametrize("case", ["plain", "ids", "nonfinite"])
+def test_unsorted_host_results_written_by_the_recheck(ctx, orc, d, case):
+    """Host results without sorting come straight from the recheck (it writes each edge as
+    input ids u < v and its weight into the pinned staging block): the same edges and
+    weight bits as the oracle's, with caller ids and with rows left out for NaNs."""
+    rng = np.random.default_rng(70 + d)
+    n = 6000
+    centres = rng.uniform(-10, 10, size=(12, d))
+    x = (centres[rng.integers(0, 12, n)] + rng.normal(size=(n, d))).astype(np.float32)
+    r = np.float32(1.5 * np.sqrt(d))
+    ids = None
+    if case == "nonfinite":
+        x[rng.choice(n, 25, replace=False), rng.integers(0, d, 25)] = np.nan
+    want = orc.eps_graph_l2(x, r)
+    if case == "ids":
+        ids = (rng.permutation(n).astype(np.int64) * 7 + 11)
+        u, v = ids[want[0]], ids[want[1]]
+        want = (np.minimum(u, v), np.maximum(u, v), want[2])
+        o = np.lexsort((want[1], want[0]))
+        want = tuple(a[o] for a in want)
+    u, v, w = ctx.eps_graph_l2(x, r, mode="bf16", ids=ids, sort=False)
+    assert (u < v).all()
+    o = np.lexsort((v, u))
+    assert same((u[o], v[o], w[o]), want)

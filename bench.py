@@ -56,34 +56,48 @@ def config(extra=None, n=N_POINTS):
 # ----------------------------------------------------------------------------- clocks
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi clocks and throttle reasons, sampled every 25 ms with nvidia-smi's own
+    timestamps.  start() launches the sampler before the warm-up (nvidia-smi takes a
+    while to print its first sample), begin() / end() mark the timed region on the host's
+    clock, and stop() keeps the samples inside it."""
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
         self.proc = None
         self.lines: list[str] = []
         self.thread = None
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
             self.proc = None
 
+    def begin(self):
+        import datetime
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        import datetime
+        self.t1 = datetime.datetime.now()
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def stop(self) -> dict:
+        import datetime
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)  # the samples of the region's last moments
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -91,22 +105,27 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, smax, reasons = [], [], set()
+        sm, smax, reasons, total = [], [], set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 8:
+            if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[0]))
-                smax.append(float(parts[1]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                clk, cmax = float(parts[1]), float(parts[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[4:8]):
+            total += 1
+            if self.t0 and self.t1 and not (self.t0 <= ts <= self.t1):
+                continue
+            sm.append(clk)
+            smax.append(cmax)
+            for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_all": total, "interval_ms": 25}
 
 
 # ----------------------------------------------------------------------------- CPU leg
@@ -267,7 +286,7 @@ def job_value(units_per_rank: int, world: int, steps: int, ms: float) -> float:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp32-steps", type=int, default=2)
@@ -318,16 +337,17 @@ def main():
         return e.count
 
     # ---- BF16 tensor-core form: warm-up, then K timed steps on the library's stream
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         edges = step(1)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     gram_ms, launches, tile_pairs, cands = [], [], [], []
     torch.cuda.synchronize()
+    clocks.begin()
     ev0.record(stream)
     for _ in range(args.steps):
         edges = step(1)
@@ -338,6 +358,7 @@ def main():
         cands.append(st["candidates"])
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist, f"cuda:{local}")
     ms_step = ms / args.steps
@@ -495,16 +516,17 @@ def run_secondary(args, world, rank, local):
         err_edges = lambda: ctx._edges_out(ctx.eps_graph_l2_raw(xh.data_ptr(), None, n, d, radius, 1, 0))
         h2d = n * d * 4
         d2h_per_unit = 8 + 4
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         units = step()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches, stats = [], []
     torch.cuda.synchronize()
+    clocks.begin()
     ev0.record(stream)
     for _ in range(args.steps):
         units = step()
@@ -513,6 +535,7 @@ def run_secondary(args, world, rank, local):
         stats.append(st)
     ev1.record(stream)
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist, dev)
     value = job_value(units, world, args.steps, ms)

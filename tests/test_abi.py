@@ -59,3 +59,34 @@ def test_unchanged_reference_drivers_build_against_the_dropin_headers():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin-drivers"], check=True)
     for d in ("systolic", "landmark", "rips"):
         assert os.path.exists(os.path.join(ROOT, "oracle", "_build", "dropin_" + d))
+
+
+@pytest.mark.parametrize("m", [1000, 1_500_000])
+def test_graph_text_of_the_dropin_writer(tmp_path, m):
+    """Graph::write_file (the drivers' collective form) prints each edge as
+    "u v w" with w in printf's %.6g, sorted; above 2^20 edges the text is formatted in
+    blocks on several host threads and must come out the same."""
+    import subprocess
+    import numpy as np
+    exe = str(tmp_path / "graph_text_check")
+    shim = os.path.join(ROOT, "rnng_gb300", "mpi_shim")
+    import rnng_gb300
+    rnng_gb300.build.build()
+    lib = os.path.dirname(rnng_gb300.LIB_PATH)
+    subprocess.run(["g++", "-O2", "-std=c++20", "-I" + shim, "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "graph_text_check.cpp"), os.path.join(shim, "mpi_shim.cpp"),
+                    "-L" + lib, "-lrnng_gpu", "-Wl,-rpath," + lib, "-pthread", "-o", exe], check=True)
+    out = str(tmp_path / "g.mtx")
+    subprocess.run([exe, str(m), out], check=True)
+    # the same edges in Python, sorted as the writer sorts them
+    s = 12345
+    mask = (1 << 64) - 1
+    rows = []
+    for i in range(m):
+        s = (s * 6364136223846793005 + 1442695040888963407) & mask
+        u, v = i // 7, (s >> 33) % 1000003
+        w = np.float32((s >> 40) / (1 << 12) * (1e-3 if i % 5 == 0 else 1.0))
+        rows.append((u, v, np.float32(i % 97) if i % 11 == 0 else w))
+    rows.sort(key=lambda r: (r[0], r[1], float(r[2])))
+    want = "%% %d %d %d\n" % (m // 7 + 1, m // 7 + 1, m) + "".join("%d %d %.6g\n" % (u, v, float(w)) for u, v, w in rows)
+    assert open(out).read() == want

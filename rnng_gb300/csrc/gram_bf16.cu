@@ -1877,9 +1877,14 @@ void run_tiles_bf16(rnng_ctx* c, Layout& L, EdgeOut& E)
         // every candidate can be an edge: room for all of them in the pinned staging block,
         // written through its device address
         const unsigned long long cap = std::max<unsigned long long>(ncand, 1);
-        char* h = (char*)host_stage(c, (size_t)cap * (2 * sizeof(int64_t) + sizeof(float)));
+        char* h = nullptr;
+        try {
+            h = (char*)host_stage(c, (size_t)cap * (2 * sizeof(int64_t) + sizeof(float)));
+        } catch (const Error&) {
+            h = nullptr;  // no pinned block that large: the results go the usual way
+        }
         void* dptr = nullptr;
-        if (cudaHostGetDevicePointer(&dptr, h, 0) == cudaSuccess && dptr) {
+        if (h && cudaHostGetDevicePointer(&dptr, h, 0) == cudaSuccess && dptr) {
             E.hu = reinterpret_cast<int64_t*>(h);
             E.hv = E.hu + cap;
             E.hw = reinterpret_cast<float*>(E.hv + cap);

@@ -1,4 +1,5 @@
-"""The allocation-free entry point (rnng_eps_graph_l2_static) against the regular one.
+"""The allocation-free entry point (rnng_eps_graph_l2_static) against the regular one
+and the oracle.
 
 Callers that may not allocate device memory when they need the graph (a plugin in a
 process whose device memory belongs to a framework's pool, a real-time loop that must
@@ -31,6 +32,7 @@ def _static_call(lib, xd, ids, n, d, r, u, v, w, cap):
 def test_static_matches_regular_entry_point_twice():
     import torch
 
+    import oracle
     import rnng_gb300
     from rnng_gb300 import synth
 
@@ -39,6 +41,9 @@ def test_static_matches_regular_entry_point_twice():
     r = np.float32(4.5)
     with rnng_gb300.Context(0) as ctx:
         want = ctx.eps_graph_l2(x, r, mode="bf16")
+    ref = oracle.eps_graph_l2(x, r)
+    assert np.array_equal(want[0], ref[0]) and np.array_equal(want[1], ref[1])
+    assert np.array_equal(want[2].view(np.uint32), ref[2].view(np.uint32))
     assert want[0].size > 500
     n, d = x.shape
     xd = torch.from_numpy(x).cuda()

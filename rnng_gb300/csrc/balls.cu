@@ -335,11 +335,17 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
         const int total = nitems * d;
         ld = tile_row_stride(d);
         if ((d & 3) == 0) {
+            // asynchronous 16-byte copies, all of the tile's in flight at once (a loop that
+            // loads and then stores keeps about one load per thread in flight, and the tile
+            // then arrives at the pace of the memory latency)
+            const int nq = d >> 2;
             const float4* s4 = reinterpret_cast<const float4*>(src);
             for (int i = threadIdx.x; i < total / 4; i += blockDim.x) {
-                const int r = (4 * i) / d, k = (4 * i) % d;  // d % 4 == 0: the four stay in row r
-                *reinterpret_cast<float4*>(tile_rows + r * ld + k) = __ldg(s4 + i);
+                const int r = i / nq, q = i - r * nq;  // d % 4 == 0: the four stay in row r
+                cp_async16(tile_rows + r * ld + 4 * q, s4 + i);
             }
+            cp_async_commit();
+            cp_async_wait<0>();
         } else {
             for (int i = threadIdx.x; i < total; i += blockDim.x) tile_rows[(i / d) * ld + i % d] = __ldg(src + i);
         }
@@ -396,8 +402,10 @@ __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __re
         const float4* c4 = reinterpret_cast<const float4*>(tcen);
         for (int e = threadIdx.x; e < m * nq; e += blockDim.x) {
             const int i = e / nq, q = e - i * nq;
-            *reinterpret_cast<float4*>(items + i * ld + 4 * q) = __ldg(c4 + (t0 * kTileBalls + src_ball[i]) * nq + q);
+            cp_async16(items + i * ld + 4 * q, c4 + (t0 * kTileBalls + src_ball[i]) * nq + q);
         }
+        cp_async_commit();
+        cp_async_wait<0>();
     } else {
         items = work + s * (int64_t)kSuper * kTileBalls * d;
         ld = d;

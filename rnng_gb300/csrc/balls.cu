@@ -197,6 +197,43 @@ __device__ __forceinline__ float row_dist(const float* __restrict__ x, const flo
     return sqrtf((s0 + s1) + (s2 + s3));
 }
 
+// One item's row for the greedy's distance walks.  NQ = 0: read from memory at every walk
+// (row_dist).  NQ > 0 (d = 4 NQ, every row the walks meet on a 16-byte boundary): held in
+// registers as NQ float4, so a walk reads only the other row; the arithmetic is
+// row_dist's 16-byte form, so the distances are the same floats.
+template <int NQ>
+struct ItemRow {
+    float4 x[NQ];
+    __device__ __forceinline__ void load(const float* __restrict__ p)
+    {
+        const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) x[q] = p4[q];
+    }
+    __device__ __forceinline__ float dist(const float* __restrict__ v, int) const
+    {
+        const float4* v4 = reinterpret_cast<const float4*>(v);
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const float4 b = v4[q];
+            const float t0 = x[q].x - b.x, t1 = x[q].y - b.y, t2 = x[q].z - b.z, t3 = x[q].w - b.w;
+            s0 = fmaf(t0, t0, s0);
+            s1 = fmaf(t1, t1, s1);
+            s2 = fmaf(t2, t2, s2);
+            s3 = fmaf(t3, t3, s3);
+        }
+        return sqrtf((s0 + s1) + (s2 + s3));
+    }
+};
+
+template <>
+struct ItemRow<0> {
+    const float* x;
+    __device__ __forceinline__ void load(const float* __restrict__ p) { x = p; }
+    __device__ __forceinline__ float dist(const float* __restrict__ v, int d) const { return row_dist(x, v, d); }
+};
+
 // block-wide (max value, index) with ties to the smaller index; result in st.pick / st.pick_v
 __device__ __forceinline__ void cover_argmax(CoverState& st, float v, int i)
 {
@@ -232,15 +269,19 @@ __device__ __forceinline__ void cover_argmax(CoverState& st, float v, int i)
 // Up to K groups of the n items; centres into cen[K][d] (global, owned by the block),
 // radii into rad[K] (-1: no group).  `cbuf` is d floats of shared memory for the centroid.
 // With `sums` (K d floats of shared memory, or null) the group centroids take one pass over
-// the items instead of one per group.
-__device__ void cover_groups(CoverState& st, const float* __restrict__ src, int ld, const float* __restrict__ irad,
-                             int n, int d, int K, float grow, float* __restrict__ cbuf, float* __restrict__ sums,
-                             float* __restrict__ cen, float* __restrict__ rad)
+// the items instead of one per group.  NQ > 0 (ItemRow): d = 4 NQ, and src, ld, cbuf and
+// cen keep every row on a 16-byte boundary.
+template <int NQ>
+__device__ __forceinline__ void cover_groups(CoverState& st, const float* __restrict__ src, int ld,
+                                             const float* __restrict__ irad, int n, int d, int K, float grow,
+                                             float* __restrict__ cbuf, float* __restrict__ sums,
+                                             float* __restrict__ cen, float* __restrict__ rad)
 {
     // item r is src[r ld .. r ld + d)
     const int t = threadIdx.x;
     const bool mine = t < n;
-    const float* xr = src + (int64_t)(mine ? t : 0) * ld;
+    ItemRow<NQ> xr;
+    xr.load(src + (int64_t)(mine ? t : 0) * ld);
     const float ir = (mine && irad) ? irad[t] : 0.f;
     // centroid of all items
     for (int k = t; k < d; k += blockDim.x) {
@@ -253,7 +294,7 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
         st.count[t] = 0;
     }
     __syncthreads();
-    float dm = mine ? row_dist(xr, cbuf, d) + ir : -1.f;
+    float dm = mine ? xr.dist(cbuf, d) + ir : -1.f;
     cover_argmax(st, dm, t);
     int ng = 0;
     int lab = 0;
@@ -261,7 +302,7 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
         const int j = st.pick;
         if (ng > 0 && !(st.pick_v > 0.f)) break;  // every item coincides with a centre
         if (mine) {
-            const float dj = row_dist(xr, src + (int64_t)j * ld, d) + ir;
+            const float dj = xr.dist(src + (int64_t)j * ld, d) + ir;
             if (ng == 0 || dj < dm) {
                 dm = dj;
                 lab = ng;
@@ -298,7 +339,7 @@ __device__ void cover_groups(CoverState& st, const float* __restrict__ src, int 
     }
     __syncthreads();
     if (mine) {
-        const float rr = row_dist(xr, cen + (int64_t)lab * d, d) + ir;
+        const float rr = xr.dist(cen + (int64_t)lab * d, d) + ir;
         atomicMax(&st.rad_bits[lab], __float_as_uint(rr));
     }
     __syncthreads();
@@ -316,7 +357,8 @@ __host__ __device__ constexpr int tile_row_stride(int d) { return (d & 3) == 0 ?
 // unused).  With staged = true the tile's rows are first copied to shared memory (rows
 // tile_row_stride(d) floats apart), which every pass of the greedy then reads.  Dynamic
 // shared memory: d floats (centroid), kTileBalls d floats with use_sums (group sums), and
-// kTile tile_row_stride(d) floats when staged.
+// kTile tile_row_stride(d) floats when staged.  NQ > 0: d = 4 NQ and staged (cover_groups).
+template <int NQ>
 __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __restrict__ Xs, int64_t n, int d,
                                                               float grow, bool staged, bool use_sums,
                                                               float* __restrict__ cen, float* __restrict__ rad)
@@ -352,13 +394,15 @@ __global__ void __launch_bounds__(kCoverThreads) k_tile_balls(const float* __res
         __syncthreads();
         src = tile_rows;
     }
-    cover_groups(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, use_sums ? sums : nullptr,
+    cover_groups<NQ>(st, src, ld, nullptr, nitems, d, kTileBalls, grow, cbuf, use_sums ? sums : nullptr,
                  cen + t * kTileBalls * d, rad + t * kTileBalls);
 }
 
 // One block per super-tile: kSuperBalls balls over its tiles' valid balls (items with
 // their radii).  Dynamic shared memory: d floats, plus kSuperBalls d with use_sums, plus
 // the staged ball centres (64 (d + 4) floats) when d is a multiple of 4 up to 128.
+// NQ > 0: d = 4 NQ (staged).
+template <int NQ>
 __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __restrict__ tcen,
                                                                const float* __restrict__ trad, int64_t T, int d,
                                                                float grow, bool use_sums, float* __restrict__ work,
@@ -414,7 +458,7 @@ __global__ void __launch_bounds__(kCoverThreads) k_super_balls(const float* __re
                 items[(int64_t)i * d + j] = tcen[(t0 * kTileBalls + src_ball[i]) * (int64_t)d + j];
     }
     __syncthreads();
-    cover_groups(st, items, ld, irad, m, d, kSuperBalls, grow, cbuf, sums, scen + s * kSuperBalls * d,
+    cover_groups<NQ>(st, items, ld, irad, m, d, kSuperBalls, grow, cbuf, sums, scen + s * kSuperBalls * d,
                  srad + s * kSuperBalls);
 }
 
@@ -964,6 +1008,23 @@ void chain_leaves(rnng_ctx* c, const float* lm_rows, int d, const int32_t* nchil
     RNNG_CUDA(cudaGetLastError());
 }
 
+// The two cover levels (tile balls, then super balls over them) of one instance.
+template <int NQ>
+static void launch_covers(rnng_ctx* c, const Layout& L, float grow, bool staged, bool tsums, bool ssums, size_t tsm,
+                          size_t ssm)
+{
+    cudaStream_t s = c->stream;
+    RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    RNNG_CUDA(cudaFuncSetAttribute(k_super_balls<NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
+    k_tile_balls<NQ><<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, tsums,
+                                                               c->tile_lo.as<float>(), c->tile_hi.as<float>());
+    ++c->launches;
+    k_super_balls<NQ><<<(unsigned)L.S, kCoverThreads, ssm, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T,
+                                                                L.d, grow, ssums, c->pivots.as<float>(),
+                                                                c->super_lo.as<float>(), c->super_hi.as<float>());
+    ++c->launches;
+}
+
 void build_covers(rnng_ctx* c, Layout& L)
 {
     cudaStream_t s = c->stream;
@@ -983,14 +1044,15 @@ void build_covers(rnng_ctx* c, Layout& L)
                        (staged ? sizeof(float) * kTile * (size_t)tile_row_stride(L.d) : 0);
     const size_t ssm = csm + (ssums ? sizeof(float) * kSuperBalls * (size_t)L.d : 0) +
                        ((L.d & 3) == 0 && L.d <= 128 ? sizeof(float) * kSuper * kTileBalls * (size_t)(L.d + 4) : 0);
-    RNNG_CUDA(cudaFuncSetAttribute(k_tile_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
-    RNNG_CUDA(cudaFuncSetAttribute(k_super_balls, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm));
-    k_tile_balls<<<(unsigned)L.T, kCoverThreads, tsm, s>>>(L.Xs, L.n, L.d, grow, staged, tsums,
-                                                           c->tile_lo.as<float>(), c->tile_hi.as<float>());
-    ++c->launches;
-    k_super_balls<<<(unsigned)L.S, kCoverThreads, ssm, s>>>(c->tile_lo.as<float>(), c->tile_hi.as<float>(), L.T, L.d,
-                                                            grow, ssums, c->pivots.as<float>(), c->super_lo.as<float>(),
-                                                            c->super_hi.as<float>()); ++c->launches;
+    // staged rows of 8, 16, 32, 64 or 128 dimensions: each thread's own row in registers
+    switch (staged && (L.d & 3) == 0 ? L.d : 0) {
+        case 8: launch_covers<2>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+        case 16: launch_covers<4>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+        case 32: launch_covers<8>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+        case 64: launch_covers<16>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+        case 128: launch_covers<32>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+        default: launch_covers<0>(c, L, grow, staged, tsums, ssums, tsm, ssm); break;
+    }
     RNNG_CUDA(cudaGetLastError());
 }
 

@@ -316,6 +316,84 @@ class VoronoiCell : public PointContainer<Atom_>
 
 namespace rnng_dropin {
 
+// Map from Index keys to non-negative Index values for the lookups made per query and per
+// replayed neighbour: open addressing with linear probing in a power-of-two table at most
+// half full, keys and values side by side (one cache line per lookup, where the node
+// chasing of std::unordered_map dominated the searches' replay).  The one key value that
+// marks free slots is stored beside the table.
+class FlatIndexMap
+{
+  public:
+    void reserve(Index n)
+    {
+        size_t want = 16;
+        while (want < 2 * (size_t)std::max<Index>(n, 0)) want *= 2;
+        if (want > slots.size()) rehash(want);
+    }
+
+    // Inserts (key, value) unless the key is present; returns whether it was inserted.
+    bool emplace(Index key, Index value)
+    {
+        if (key == kFree) {
+            if (has_free_key) return false;
+            has_free_key = true;
+            free_key_value = value;
+            return true;
+        }
+        if (2 * (count + 1) > slots.size()) rehash(std::max<size_t>(16, 2 * slots.size()));
+        for (size_t h = home(key);; h = (h + 1) & mask) {
+            Slot& s = slots[h];
+            if (s.key == kFree) {
+                s = Slot{key, value};
+                ++count;
+                return true;
+            }
+            if (s.key == key) return false;
+        }
+    }
+
+    // The key's value, or -1.
+    Index find(Index key) const
+    {
+        if (key == kFree) return has_free_key ? free_key_value : -1;
+        if (slots.empty()) return -1;
+        for (size_t h = home(key);; h = (h + 1) & mask) {
+            const Slot& s = slots[h];
+            if (s.key == key) return s.value;
+            if (s.key == kFree) return -1;
+        }
+    }
+
+    size_t size() const { return count + (has_free_key ? 1 : 0); }
+
+  private:
+    struct Slot {
+        Index key, value;
+    };
+    static constexpr Index kFree = std::numeric_limits<Index>::min();
+
+    // Fibonacci hashing: the top bits of key x 2^64 / golden ratio
+    size_t home(Index key) const { return (size_t)(((uint64_t)key * 0x9E3779B97F4A7C15ull) >> shift); }
+
+    void rehash(size_t n)
+    {
+        std::vector<Slot> old(n, Slot{kFree, 0});
+        old.swap(slots);  // slots: the new free table; old: the entries to insert again
+        mask = n - 1;
+        shift = 64;
+        for (size_t v = n; v > 1; v >>= 1) --shift;
+        count = 0;
+        for (const Slot& s : old)
+            if (s.key != kFree) emplace(s.key, s.value);
+    }
+
+    std::vector<Slot> slots;
+    size_t mask = 0, count = 0;
+    int shift = 64;
+    bool has_free_key = false;
+    Index free_key_value = -1;
+};
+
 // Unordered edges (a < b, container rows) of the epsilon graph of a container.
 struct RowEdges {
     std::vector<int64_t> u, v;
@@ -365,21 +443,21 @@ template <class Atom>
 struct GraphCache {
     Real radius = 0;
     PointContainer<Atom> pts;
-    std::unordered_map<Index, Index> row_of_id;
+    FlatIndexMap row_of_id;
     IndexVector rowptr, nbr;
     RealVector w;
 
     // Row holding a point with the same id and the same atoms, or -1.
     Index find(const Point<Atom>& p) const
     {
-        auto it = row_of_id.find(p.id());
-        if (it == row_of_id.end()) return -1;
-        const Point<Atom> q = pts[it->second];
+        const Index row = row_of_id.find(p.id());
+        if (row < 0) return -1;
+        const Point<Atom> q = pts[row];
         if (q.size() != p.size() || !std::equal(p.begin(), p.end(), q.begin(), [](Atom a, Atom b) {
                 return std::memcmp(&a, &b, sizeof(Atom)) == 0;
             }))
             return -1;
-        return it->second;
+        return row;
     }
 
     // Rows of all points of a container, if the graph holds every one of them.
@@ -412,7 +490,7 @@ std::shared_ptr<const GraphCache<Atom>> build_graph(const PointContainer<Atom>& 
     const Index n = pts.num_points();
     bool unique_ids = true;
     g->row_of_id.reserve(n);
-    for (Index i = 0; i < n && unique_ids; ++i) unique_ids = g->row_of_id.emplace(pts[i].id(), i).second;
+    for (Index i = 0; i < n && unique_ids; ++i) unique_ids = g->row_of_id.emplace(pts[i].id(), i);
     assert((unique_ids));  // RNNG's ids are unique; the lookup by id relies on it
     const RowEdges e = eps_graph_rows(pts, radius);
     g->rowptr.assign(n + 1, 0);

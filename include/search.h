@@ -24,7 +24,7 @@ namespace rnng_dropin {
 // of the graph, a hash map when it is a small part of it (one Voronoi cell).
 struct LocalIndex {
     IndexVector dense;
-    std::unordered_map<Index, Index> sparse;
+    FlatIndexMap sparse;
     bool use_dense = false;
 
     void build(const IndexVector& rows, Index graph_rows)
@@ -42,8 +42,7 @@ struct LocalIndex {
     Index operator[](Index row) const
     {
         if (use_dense) return dense[row];
-        auto it = sparse.find(row);
-        return it == sparse.end() ? -1 : it->second;
+        return sparse.find(row);
     }
 };
 

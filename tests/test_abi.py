@@ -61,6 +61,23 @@ def test_unchanged_reference_drivers_build_against_the_dropin_headers():
         assert os.path.exists(os.path.join(ROOT, "oracle", "_build", "dropin_" + d))
 
 
+def test_dropin_lookup_tables(tmp_path):
+    """The open-addressing map behind the drop-in searches' id and row lookups (and
+    LocalIndex in both forms) agrees with std::unordered_map on sequential, random,
+    negative and extreme keys, with and without reserve."""
+    import subprocess
+    exe = str(tmp_path / "index_map_check")
+    shim = os.path.join(ROOT, "rnng_gb300", "mpi_shim")
+    import rnng_gb300
+    rnng_gb300.build.build()
+    lib = os.path.dirname(rnng_gb300.LIB_PATH)
+    subprocess.run(["g++", "-O2", "-std=c++20", "-I" + shim, "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "index_map_check.cpp"), os.path.join(shim, "mpi_shim.cpp"),
+                    "-L" + lib, "-lrnng_gpu", "-Wl,-rpath," + lib, "-pthread", "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
 @pytest.mark.parametrize("m", [1000, 1_500_000])
 def test_graph_text_of_the_dropin_writer(tmp_path, m):
     """Graph::write_file (the drivers' collective form) prints each edge as

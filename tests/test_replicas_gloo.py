@@ -57,3 +57,33 @@ def test_single_process_and_reference_arm_on_other_ranks(capsys):
         warmup, steps, points = 3, 1, bench.N_POINTS
     bench.run_reference(Args, world=2, rank=1)  # rank 1 of the reference arm does no work
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_on_rank_zero(capsys, monkeypatch):
+    """Rank 0 of the reference arm prints one JSON line with the GPU arm's metric and unit,
+    the CPU baseline it timed (RNNG's landmark pipeline restated in C, kind "port"), no
+    host-device bytes, and the same edges as the brute-force restatement (a 4,000-point
+    prefix of the descriptors stands in for the 100,000 of a bench run)."""
+    import json
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    from rnng_gb300 import synth
+    x = synth.descriptor(n=4000, d=bench.DIM)
+    monkeypatch.setattr(bench, "workload", lambda n=bench.N_POINTS: (x, synth.EPS_K2))
+
+    class Args:
+        warmup, steps, points, workload = 3, 2, bench.N_POINTS, "k2"
+    bench.run_reference(Args, world=1, rank=0)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["higher_is_better"] is True and d["steps"] == 2 and d["warmup"] == 3 and d["value"] > 0
+    assert d["e2e"] == {"value": d["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["cores"] >= 1
+    assert "first 4000 points" in cb["sample"]
+    u, _, _ = oracle.eps_graph_l2(x, synth.EPS_K2)
+    assert f"{u.size} edges" in cb["sample"]
